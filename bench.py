@@ -1,0 +1,329 @@
+"""Throughput benchmark of the lime_gb300 density-matrix propagator.
+
+Workload: the static-disorder ensemble — 4096 realisations of a 64-site
+Frenkel exciton chain (site energies ~ N(0, 0.05), J = -0.1, open ends),
+pure dephasing gamma_b ~ U(0.005, 0.02), rho0 = |0><0|, dt = 0.05, site
+populations recorded.  A bench "step" is one RK4 time step of the whole
+ensemble; ``--steps K`` RK4 steps are timed (the full workload is 4000).
+
+Metric: instance-steps/s (one RK4 step of one density matrix).
+
+Arms:
+  (default)          lime_gb300 CUDA path (``--path split`` once available,
+                     else the plain FP64 kernel); also reports the plain FP64
+                     GPU rate, the roofline of the dominant kernel, an
+                     end-to-end number through the public API with host
+                     buffers, and the CPU oracle baseline.
+  --impl reference   the reference algorithm on the host cores (the NumPy
+                     restatement in oracle/, one process per core).
+
+Multi-GPU: instances are independent, so N ranks run disjoint slices of the
+ensemble (weak scaling, no collective); rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'batched rho RK4 instance-steps/s'
+N_SITES = 64
+BATCH = 4096
+DT = 0.05
+FULL_STEPS = 4000
+CPU_SAMPLE_STEPS = 150   # ~10 s of oracle work per host core
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=None)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='lime', choices=['lime', 'reference'])
+    p.add_argument('--path', default='auto', choices=['auto', 'fp64', 'split'])
+    p.add_argument('--batch', type=int, default=BATCH)
+    p.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
+    p.add_argument('--no-e2e', action='store_true')
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(
+                ['nvidia-smi', '-i', str(self.index), '--query-gpu=' + q,
+                 '--format=csv,noheader,nounits', '-lms', '200'],
+                stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': [], 'samples': 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), samples=len(sm))
+        out['reasons'] = sorted(reasons)
+        return out
+
+
+def flush_l2(torch, dev):
+    buf = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    buf.fill_(1)
+    del buf
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# ------------------------------------------------------------------ workload
+def make_workload(batch, rank=0, world=1):
+    import numpy as np
+    from lime_gb300 import chains
+    w = chains.disorder_ensemble(n=N_SITES, batch=BATCH if batch is None else batch, n_steps=FULL_STEPS)
+    lo = rank * len(w['H']) // world
+    hi = (rank + 1) * len(w['H']) // world
+    H = w['H'][lo:hi]
+    g = w['gamma'][lo:hi]
+    # K = n diagonal collapse operators sqrt(gamma_b)|k><k|, given by their diagonals
+    l = np.zeros((hi - lo, N_SITES, N_SITES), dtype=np.complex128)
+    idx = np.arange(N_SITES)
+    l[:, idx, idx] = np.sqrt(g)[:, None]
+    pops = np.eye(N_SITES, dtype=np.complex128)  # diagonals of the population observables
+    return dict(H=H, l=l, rho0=w['rho0'], pops=pops, gamma=g)
+
+
+def gpu_arm(args, rank, world, local):
+    import numpy as np
+    import torch
+    from lime_gb300 import _native as nat
+    from lime_gb300 import build as lbuild
+    from lime_gb300 import chains, engine
+    from lime_gb300.engine import DiagonalOps
+
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=dev)
+    lbuild.build()
+    nat.require_device()
+
+    path = 'fp64' if args.path in ('auto', 'fp64') else args.path
+    K = args.steps if args.steps is not None else (FULL_STEPS if path == 'split' else 8)
+    W = max(3, args.warmup)
+    wl = make_workload(args.batch, rank, world)
+    B = wl['H'].shape[0]
+    pop_ops = [np.diag(wl['pops'][k]) for k in range(N_SITES)]
+
+    gen = engine.LindbladGenerator.build(wl['H'], [DiagonalOps(wl['l'])], device=dev)
+    rho0 = torch.as_tensor(np.broadcast_to(wl['rho0'], (B, N_SITES, N_SITES)).copy(),
+                           dtype=torch.complex128, device=dev)
+    obs_every = max(1, K // 100)
+
+    def run(nsteps, events=None):
+        return engine.propagate(gen, rho0, DT, nsteps, pop_ops, precision=path,
+                                obs_every=max(1, min(obs_every, nsteps)), events=events)
+
+    run(W)
+    torch.cuda.synchronize()
+    flush_l2(torch, dev)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+    n0 = nat.launch_count()
+    with ClockSampler(local) as clk:
+        ev0.record()
+        obs, _, _ = run(K, events=kev)
+        ev1.record()
+        torch.cuda.synchronize()
+    launches = nat.launch_count() - n0
+    t = ev0.elapsed_time(ev1) / 1e3
+    tk = kev[0].elapsed_time(kev[1]) / 1e3
+    if world > 1:
+        tt = torch.tensor([t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t = float(tt.item())
+    total_instances = B * world
+    value = total_instances * K / t
+    clocks = clk.summary()
+
+    # plain FP64 GPU rate on the same ensemble (the metric's denominator)
+    fp64_rate = None
+    if path == 'fp64':
+        fp64_rate = value
+    e2e = None
+    if not args.no_e2e and rank == 0:
+        e2e = e2e_leg(wl, K, path, dev)
+    cpu = None
+    if not args.no_cpu and rank == 0 and world == 1:
+        from oracle import pool
+        rate, cores, wall = pool.ensemble_rate(n=N_SITES, n_steps=CPU_SAMPLE_STEPS)
+        cpu = {'value': rate, 'unit': 'instance-steps/s', 'cores': cores, 'kind': 'port',
+               'sample': '%d realisations x %d RK4 steps, one process per core (%.1f s)'
+                         % (cores, CPU_SAMPLE_STEPS, wall)}
+
+    # roofline of the dominant kernel
+    peaks = measured_peaks()
+    flop_per_inst_step = 64 * N_SITES ** 3   # 2 complex N^3 GEMMs per RHS, 4 RHS
+    achieved_tf = B * K * flop_per_inst_step / tk / 1e12
+    if path == 'fp64':
+        roof = {'bound': 'fp64', 'achieved': achieved_tf, 'peak': 1.25, 'unit': 'TFLOP/s',
+                'frac': achieved_tf / 1.25, 'traffic': None,
+                'peak_source': 'nominal GB300 FP64 (no measured FP64 peak available)'}
+    else:
+        pk = peaks.get('bf16_tflops_sustained') or 1700.0
+        roof = {'bound': 'tensor', 'achieved': achieved_tf, 'peak': pk, 'unit': 'TFLOP/s',
+                'frac': achieved_tf / pk, 'traffic': None,
+                'peak_source': 'measured bf16 sustained' if peaks else 'fallback'}
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'instance-steps/s', 'n_gpus': world,
+        'steps': K, 'warmup': W, 'ms_per_step': t / K * 1e3, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f64' if path == 'fp64' else 'f32 (split 16-bit tensor operands)',
+        'data': 'synthetic (seeded disorder ensemble)',
+        'config': {'workload': 'dephasing exciton-chain ensemble N=64, 4096 realisations, '
+                               'dt=0.05 (4000-step workload; K steps timed)',
+                   'n_sites': N_SITES, 'batch': total_instances, 'path': path,
+                   'l2': 'flushed before the timed launch; rho stays on chip across steps',
+                   'observables': 'site populations every %d steps' % obs_every},
+        'kernel_s': tk,
+        'fp64_gpu_instance_steps_per_s': fp64_rate,
+        'gpu_launches': launches,
+        'clocks': clocks,
+        'roofline': roof,
+        'e2e': e2e,
+        'cpu_baseline': cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+def e2e_leg(wl, K, path, dev):
+    """Same metric through the public API with host (pinned) buffers."""
+    import numpy as np
+    import torch
+    from lime_gb300.oqs import Lindblad_solver, DiagonalOps
+    B = wl['H'].shape[0]
+    H = torch.as_tensor(wl['H']).pin_memory()
+    l = torch.as_tensor(wl['l']).pin_memory()
+    rho0 = wl['rho0']
+    pops = [np.diag(wl['pops'][k]) for k in range(N_SITES)]
+    nout = max(1, K // 100)
+    sol = Lindblad_solver(H, c_ops=[DiagonalOps(l)], precision=path)
+    sol.evolve(rho0, dt=DT, Nt=2, e_ops=pops, store_states=False)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = sol.evolve(rho0, dt=DT, Nt=K, e_ops=pops, nout=nout, store_states=False)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    h2d = H.numel() * 16 + l.numel() * 16 + rho0.size * 16 + N_SITES * N_SITES * 16
+    d2h = res.observables.nbytes + np.asarray(res.rholist).nbytes
+    return {'value': B * K / t, 'unit': 'instance-steps/s',
+            'h2d_bytes_per_step': h2d / K, 'd2h_bytes_per_step': d2h / K,
+            'api': 'lime_gb300.oqs.Lindblad_solver.evolve (numpy/pinned host arrays in, '
+                   'numpy Result out)'}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    from oracle import pool
+    K = args.steps if args.steps is not None else FULL_STEPS
+    W = max(3, args.warmup)
+    rate, cores, wall = pool.ensemble_rate(n=N_SITES, n_steps=CPU_SAMPLE_STEPS)
+    value = rate
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'instance-steps/s', 'n_gpus': world,
+        'steps': K, 'warmup': W, 'ms_per_step': BATCH / value * 1e3,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+        'data': 'synthetic (seeded disorder ensemble)', 'impl': 'reference',
+        'config': {'workload': 'dephasing exciton-chain ensemble N=64, 4096 realisations, '
+                               'dt=0.05 (4000-step workload)', 'n_sites': N_SITES,
+                   'batch': BATCH},
+        'cpu_baseline': {'value': value, 'unit': 'instance-steps/s', 'cores': cores,
+                         'kind': 'port',
+                         'sample': '%d realisations x %d RK4 steps, one process per core '
+                                   '(%.1f s); ms_per_step extrapolates to the 4096-instance '
+                                   'ensemble' % (cores, CPU_SAMPLE_STEPS, wall)},
+        'e2e': {'value': value, 'unit': 'instance-steps/s', 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == 'reference':
+        reference_arm(args, rank, world)
+        return
+    gpu_arm(args, rank, world, local)
+
+
+if __name__ == '__main__':
+    main()

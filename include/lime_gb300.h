@@ -1,0 +1,138 @@
+/*
+ * lime_gb300 — C ABI of the GB300 (sm_103a) open-system density-matrix
+ * propagator.
+ *
+ * The reference (binggu56/lime) is pure Python and has no FFI; each entry
+ * point below replaces the inner loop of one reference solver and is bound
+ * from Python through ctypes (lime_gb300/_native.py).  Conventions:
+ *
+ *  - Complex matrices are interleaved (re, im) pairs, row-major,
+ *    instance-major: element (b, i, j) of a [B][N][N] array sits at
+ *    ((b * stride) + i * N + j) complex elements from the base, where
+ *    ``stride`` is the per-instance stride in complex elements (0 = one
+ *    matrix shared by every instance).
+ *  - All pointers are DEVICE pointers owned by the caller.  No entry point
+ *    allocates, frees or synchronises; work is enqueued on ``stream``.
+ *  - Every entry point returns LIME_OK (0) or a negative lime_status and
+ *    never throws.  Errors found by a kernel (non-finite values, trace
+ *    drift) are written to the caller's device ``status`` word as a
+ *    bit mask (LIME_FLAG_*) and read by the caller after the stream syncs.
+ *  - Calls on different streams with disjoint buffers are independent.
+ *
+ * Physics: every propagator integrates the Lindblad generator written as
+ *     d rho/dt = -i (Heff rho - rho Heff^dag) + sum_k L_k rho L_k^dag
+ *     Heff     = H - (i/2) sum_k L_k^dag L_k
+ * (algebraically identical to -i[H, rho] + sum_k (L rho L^dag - 1/2{L^dag L, rho}),
+ * lime/oqs.py:706-723), with classic RK4 steps (lime/phys.py:636-649).
+ * Collapse operators that are diagonal (L_k = diag(l_k)) enter through the
+ * Hermitian matrix M = sum_k l_k l_k^dag:  sum_k L_k rho L_k^dag = M o rho.
+ * The propagators act on Hermitian rho; a non-Hermitian rho is propagated as
+ * its two Hermitian parts (the generator is linear and Hermiticity-preserving).
+ */
+#ifndef LIME_GB300_H
+#define LIME_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  LIME_OK = 0,
+  LIME_ERR_ARG = -1,          /* bad size, stride, pointer or alignment     */
+  LIME_ERR_UNSUPPORTED = -2,  /* valid request this build does not handle  */
+  LIME_ERR_CUDA = -3,         /* a CUDA runtime call failed                */
+  LIME_ERR_NO_DEVICE = -4,    /* no sm_103 device current                  */
+  LIME_ERR_WORKSPACE = -5,    /* workspace too small                       */
+} lime_status;
+
+/* bits of the device status word written by kernels */
+#define LIME_FLAG_NONFINITE   0x1  /* a NaN/Inf appeared in rho            */
+#define LIME_FLAG_TRACE_DRIFT 0x2  /* |Tr rho(t) - Tr rho(0)| > trace_tol   */
+#define LIME_FLAG_TIMEOUT     0x4  /* a bounded device-side wait expired    */
+
+/* ------------------------------------------------------------------ */
+/* Generator preparation                                               */
+/* ------------------------------------------------------------------ */
+
+/* Build Heff = H - (i/2) sum_k L_k^dag L_k  and  M = sum_k l_k l_k^dag.
+ * Replaces the per-RHS products dag(l).dot(l) of lime/oqs.py:716-723.
+ *   h        [B|1][n][n] complex128, stride h_stride (0 = shared)
+ *   l_dense  [B|1][k_dense][n][n] complex128 dense collapse ops, or NULL
+ *   l_diag   [B|1][k_diag][n]     complex128 diagonals of diagonal ops, or NULL
+ *   heff     [B][n][n] complex128 out
+ *   m        [B][n][n] complex128 out (zero when k_diag == 0)
+ */
+typedef struct {
+  int32_t n, batch, k_dense, k_diag;
+  const double* h;        int64_t h_stride;
+  const double* l_dense;  int64_t l_dense_stride;
+  const double* l_diag;   int64_t l_diag_stride;
+  double* heff;
+  double* m;
+} LimePrepareDesc;
+
+int lime_lindblad_prepare_f64(const LimePrepareDesc* d, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Plain FP64 Lindblad RK4                                              */
+/* ------------------------------------------------------------------ */
+
+/* RK4 propagation of B Hermitian density matrices in FP64.
+ * Replaces the time loop of _lindblad (lime/oqs.py:1590-1688) and
+ * _correlation_2p_1t (lime/oqs.py:726-800):
+ *   rho       [B][n][n] in: rho(t0); out: rho(t0 + n_steps dt)
+ *   param_batch P: instance b uses parameter set p = b % P for heff, m,
+ *             l_dense and obs_ops (0 means P = B).  A non-Hermitian input
+ *             split into its Hermitian parts runs as B = 2P instances.
+ *   heff      [P|1][n][n]           (from lime_lindblad_prepare_f64)
+ *   m         [P|1][n][n] or NULL   (diagonal collapse operators)
+ *   l_dense   [P|1][k_dense][n][n] or NULL
+ *   obs_ops   [P|1][n_obs][n][n] observables (obs_diag = 0), or their
+ *             diagonals [P|1][n_obs][n] when every observable is diagonal
+ *             (obs_diag = 1), stride obs_stride per parameter set (0 =
+ *             shared); obs_out[B][n_steps / obs_every][n_obs] receives
+ *             Tr(E rho) after steps obs_every-1, 2*obs_every-1, ...
+ *             (obs_every = 1: after every step, t = (k+1) dt, the
+ *             reference's Result.observables timing, lime/oqs.py:1674-1682)
+ *   states    [B][n_steps / states_every][n][n] or NULL: rho after steps
+ *             states_every-1, 2*states_every-1, ...
+ *   workspace caller-allocated, lime_lindblad_rk4_f64_workspace() bytes
+ *   status    one int32 on the device (OR-ed LIME_FLAG_* bits)
+ *   trace_tol trace-drift bound (<= 0 disables the check)
+ */
+typedef struct {
+  int32_t n, batch, param_batch, n_steps, k_dense, n_obs, obs_diag, obs_every, states_every;
+  double dt, trace_tol;
+  double* rho;
+  const double* heff;     int64_t heff_stride;
+  const double* m;        int64_t m_stride;
+  const double* l_dense;  int64_t l_dense_stride;
+  const double* obs_ops;  int64_t obs_stride;
+  double* obs_out;
+  double* states;
+  void* workspace;        size_t workspace_bytes;
+  int32_t* status;
+} LimeLindbladDesc;
+
+size_t lime_lindblad_rk4_f64_workspace(int32_t n, int32_t batch, int32_t k_dense);
+int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream);
+
+/* ------------------------------------------------------------------ */
+/* Library info                                                         */
+/* ------------------------------------------------------------------ */
+
+/* 0 when a device of compute capability 10.3 is current, else negative. */
+int lime_device_check(void);
+/* Cumulative number of kernels this library has enqueued (all entry points,
+ * all threads); lets a caller count the launches inside a timed region. */
+int64_t lime_launch_count(void);
+const char* lime_status_string(int status);
+int lime_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LIME_GB300_H */

@@ -1,0 +1,136 @@
+"""ctypes binding of the C ABI declared in include/lime_gb300.h.
+
+The library is the in-tree ``lime_gb300/liblime_gb300.so`` produced by
+``lime_gb300.build``.  There is no fallback: if the library is missing or no
+compute-capability-10.3 GPU is current, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'liblime_gb300.so')
+
+c_int32 = ctypes.c_int32
+c_int64 = ctypes.c_int64
+c_double = ctypes.c_double
+c_void_p = ctypes.c_void_p
+c_size_t = ctypes.c_size_t
+
+LIME_FLAG_NONFINITE = 0x1
+LIME_FLAG_TRACE_DRIFT = 0x2
+LIME_FLAG_TIMEOUT = 0x4
+
+
+class LimeError(RuntimeError):
+    """A lime_gb300 entry point returned a negative status."""
+
+    def __init__(self, status, where):
+        self.status = status
+        super().__init__('%s failed: %s (status %d)' % (where, status_string(status), status))
+
+
+class KernelFlagError(RuntimeError):
+    """A kernel raised a device status flag (non-finite values, trace drift, timeout)."""
+
+    def __init__(self, flags, where):
+        self.flags = flags
+        names = []
+        if flags & LIME_FLAG_NONFINITE:
+            names.append('non-finite values in rho')
+        if flags & LIME_FLAG_TRACE_DRIFT:
+            names.append('trace drift above tolerance')
+        if flags & LIME_FLAG_TIMEOUT:
+            names.append('device-side wait timed out')
+        super().__init__('%s: %s (flags 0x%x)' % (where, ', '.join(names) or 'unknown', flags))
+
+
+class PrepareDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('batch', c_int32), ('k_dense', c_int32), ('k_diag', c_int32),
+                ('h', c_void_p), ('h_stride', c_int64),
+                ('l_dense', c_void_p), ('l_dense_stride', c_int64),
+                ('l_diag', c_void_p), ('l_diag_stride', c_int64),
+                ('heff', c_void_p), ('m', c_void_p)]
+
+
+class LindbladDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('batch', c_int32), ('param_batch', c_int32),
+                ('n_steps', c_int32), ('k_dense', c_int32),
+                ('n_obs', c_int32), ('obs_diag', c_int32), ('obs_every', c_int32),
+                ('states_every', c_int32),
+                ('dt', c_double), ('trace_tol', c_double),
+                ('rho', c_void_p),
+                ('heff', c_void_p), ('heff_stride', c_int64),
+                ('m', c_void_p), ('m_stride', c_int64),
+                ('l_dense', c_void_p), ('l_dense_stride', c_int64),
+                ('obs_ops', c_void_p), ('obs_stride', c_int64),
+                ('obs_out', c_void_p), ('states', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t),
+                ('status', c_void_p)]
+
+
+# (name, restype, argtypes) of every exported symbol; tests check the header
+# declares exactly these.
+SIGNATURES = [
+    ('lime_lindblad_prepare_f64', c_int32, [ctypes.POINTER(PrepareDesc), c_void_p]),
+    ('lime_lindblad_rk4_f64_workspace', c_size_t, [c_int32, c_int32, c_int32]),
+    ('lime_lindblad_rk4_f64', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
+    ('lime_device_check', c_int32, []),
+    ('lime_launch_count', c_int64, []),
+    ('lime_status_string', ctypes.c_char_p, [c_int32]),
+    ('lime_version', c_int32, []),
+]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the library (without touching the GPU)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError('lime_gb300 CUDA library not found at %s; build it with '
+                           '`python -m lime_gb300.build`' % path)
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def launch_count() -> int:
+    return int(load().lime_launch_count())
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().lime_status_string(status).decode()
+    except Exception:  # pragma: no cover
+        return 'status %d' % status
+
+
+def check(status: int, where: str):
+    if status != 0:
+        raise LimeError(status, where)
+
+
+_device_ok = False
+
+
+def require_device():
+    """Raise unless a compute-capability-10.3 (GB300) device is current."""
+    global _device_ok
+    if _device_ok:
+        return load()
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError('lime_gb300 needs a CUDA GPU (sm_103a); none is available')
+    torch.cuda.init()
+    lib = load()
+    check(lib.lime_device_check(), 'lime_device_check')
+    _device_ok = True
+    return lib

@@ -1,0 +1,329 @@
+// Plain FP64 Lindblad RK4 propagator (sm_103a).
+//
+// One CTA owns one density matrix for the whole time loop: every RK4 stage is
+// a CTA-wide complex GEMM X = Heff * rho_s (register-tiled, operands staged
+// through shared memory) followed by a fused epilogue that forms
+//   f = -i (X - X^dag) + M o rho_s + sum_k L_k rho_s L_k^dag
+// and the RK4 stage combination (lime/phys.py:636-649), then the trace check
+// and the observables of lime/phys.py:837-844.  rho is Hermitian (the host
+// splits non-Hermitian inputs), so rho Heff^dag = (Heff rho)^dag and one GEMM
+// per stage gives the whole coherent + anti-Hermitian part.
+//
+// GB300 executes FP64 at a small fraction of its tensor rate, so this path is
+// DFMA-bound for every size; its job is to be exact (it is the GPU FP64
+// reference for the split-precision propagator), not fast.
+
+#include "common.cuh"
+
+namespace lime {
+namespace f64 {
+
+constexpr int kThreads = 256;
+constexpr int kKC = 16;  // k-chunk of the shared-memory tiles
+
+// Workspace layout per instance (complex elements): rs | X | acc | [Y | J]
+__host__ __device__ inline int64_t ws_mats(int k_dense) { return k_dense > 0 ? 5 : 3; }
+
+// C (+)= A * op(B), all n x n, row-major, global memory; whole CTA.
+// op(B) = B (conjb = false) or B^dag (conjb = true).
+template <int TM>
+__device__ void cta_cgemm(const double2* __restrict__ A, const double2* __restrict__ B,
+                          bool conjb, double2* __restrict__ C, bool accumulate, int n,
+                          double2* smem) {
+  constexpr int T = 16 * TM;
+  double2* As = smem;                   // [T][kKC + 1]
+  double2* Bs = smem + T * (kKC + 1);   // [kKC][T + 1]
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  for (int i0 = 0; i0 < n; i0 += T) {
+    for (int j0 = 0; j0 < n; j0 += T) {
+      double2 acc[TM][TM];
+#pragma unroll
+      for (int u = 0; u < TM; ++u)
+#pragma unroll
+        for (int v = 0; v < TM; ++v) acc[u][v] = cz();
+      for (int k0 = 0; k0 < n; k0 += kKC) {
+        for (int idx = threadIdx.x; idx < T * kKC; idx += kThreads) {
+          const int r = idx / kKC, c = idx % kKC;
+          const int gi = i0 + r, gk = k0 + c;
+          As[r * (kKC + 1) + c] = (gi < n && gk < n) ? A[(int64_t)gi * n + gk] : cz();
+        }
+        if (!conjb) {
+          for (int idx = threadIdx.x; idx < T * kKC; idx += kThreads) {
+            const int r = idx / T, c = idx % T;
+            const int gk = k0 + r, gj = j0 + c;
+            Bs[r * (T + 1) + c] = (gk < n && gj < n) ? B[(int64_t)gk * n + gj] : cz();
+          }
+        } else {
+          // op(B)[k][j] = conj(B[j][k]); read along k for coalescing
+          for (int idx = threadIdx.x; idx < T * kKC; idx += kThreads) {
+            const int c = idx / kKC, r = idx % kKC;
+            const int gk = k0 + r, gj = j0 + c;
+            Bs[r * (T + 1) + c] = (gk < n && gj < n) ? cconj(B[(int64_t)gj * n + gk]) : cz();
+          }
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < kKC; ++kk) {
+          double2 a[TM], b[TM];
+#pragma unroll
+          for (int u = 0; u < TM; ++u) a[u] = As[(ty + 16 * u) * (kKC + 1) + kk];
+#pragma unroll
+          for (int v = 0; v < TM; ++v) b[v] = Bs[kk * (T + 1) + tx + 16 * v];
+#pragma unroll
+          for (int u = 0; u < TM; ++u)
+#pragma unroll
+            for (int v = 0; v < TM; ++v) cfma(acc[u][v], a[u], b[v]);
+        }
+        __syncthreads();
+      }
+#pragma unroll
+      for (int u = 0; u < TM; ++u) {
+#pragma unroll
+        for (int v = 0; v < TM; ++v) {
+          const int gi = i0 + ty + 16 * u, gj = j0 + tx + 16 * v;
+          if (gi < n && gj < n) {
+            double2* c = C + (int64_t)gi * n + gj;
+            *c = accumulate ? cadd(*c, acc[u][v]) : acc[u][v];
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+struct RK4Args {
+  int n, param_batch, n_steps, k_dense, n_obs, obs_diag, states_every, states_per_inst, step0;
+  double dt, trace_tol;
+  double2* rho;
+  const double2* heff;    int64_t heff_stride;
+  const double2* m;       int64_t m_stride;
+  const double2* l_dense; int64_t l_dense_stride;
+  const double2* obs_ops; int64_t obs_stride;
+  double2* obs_out;       int obs_every, obs_per_inst;
+  double2* states;
+  double2* ws;
+  double* tr0;
+  int32_t* status;
+};
+
+template <int TM>
+__global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
+  extern __shared__ double2 smem[];
+  __shared__ double red[kThreads / 32];
+  const int b = blockIdx.x;
+  const int n = a.n;
+  const int64_t nn = (int64_t)n * n;
+  const int p = b % a.param_batch;
+  double2* rho = a.rho + b * nn;
+  const double2* heff = a.heff + p * a.heff_stride;
+  const double2* m = a.m ? a.m + p * a.m_stride : nullptr;
+  const double2* ld = a.l_dense ? a.l_dense + p * a.l_dense_stride : nullptr;
+  const double2* obs_ops = a.obs_ops ? a.obs_ops + p * a.obs_stride : nullptr;
+  double2* ws = a.ws + (int64_t)b * ws_mats(a.k_dense) * nn;
+  double2* rs = ws;
+  double2* X = ws + nn;
+  double2* acc = ws + 2 * nn;
+  double2* Y = ws + 3 * nn;
+  double2* J = ws + 4 * nn;
+
+  // trace at the start of the call (first chunk) for the drift check
+  if (a.step0 == 0) {
+    double t = 0.0;
+    for (int i = threadIdx.x; i < n; i += kThreads) t += rho[(int64_t)i * n + i].x;
+    t = block_sum<kThreads>(t, red);
+    if (threadIdx.x == 0) a.tr0[b] = t;
+  }
+  for (int64_t e = threadIdx.x; e < nn; e += kThreads) rs[e] = rho[e];
+  __syncthreads();
+  const double tr0 = a.tr0[b];
+
+  const double dt = a.dt, dt2 = a.dt / 2.0;
+  int flags = 0;
+  for (int step = 0; step < a.n_steps; ++step) {
+#pragma unroll 1
+    for (int s = 0; s < 4; ++s) {
+      cta_cgemm<TM>(heff, rs, false, X, false, n, smem);
+      for (int k = 0; k < a.k_dense; ++k) {
+        const double2* L = ld + k * nn;
+        cta_cgemm<TM>(L, rs, false, Y, false, n, smem);
+        cta_cgemm<TM>(Y, L, true, J, k > 0, n, smem);
+      }
+      const double cstage = (s == 2) ? dt : dt2;
+      for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        const double2 x = X[e], xt = X[(int64_t)j * n + i];
+        // -i (x - conj(xt))
+        const double2 d = make_double2(x.x - xt.x, x.y + xt.y);
+        double2 f = make_double2(d.y, -d.x);
+        const double2 r = rs[e];
+        if (m) f = cadd(f, cmul(m[e], r));
+        if (a.k_dense > 0) f = cadd(f, J[e]);
+        if (s == 0) {
+          acc[e] = f;
+          rs[e] = cadd(rho[e], cscale(f, cstage));
+        } else if (s < 3) {
+          acc[e] = cadd(acc[e], cscale(f, 2.0));
+          rs[e] = cadd(rho[e], cscale(f, cstage));
+        } else {
+          const double2 sum = cadd(acc[e], f);
+          const double2 nr = cadd(rho[e], cscale(make_double2(sum.x / 6., sum.y / 6.), dt));
+          rho[e] = nr;
+          rs[e] = nr;
+          if (!cfinite(nr)) flags |= LIME_FLAG_NONFINITE;
+        }
+      }
+      __syncthreads();
+    }
+    // observables after the step
+    const int gstep = a.step0 + step;
+    const bool obs_now = ((gstep + 1) % a.obs_every) == 0;
+    const int oslot = (gstep + 1) / a.obs_every - 1;
+    for (int o = 0; obs_now && o < a.n_obs; ++o) {
+      double sr = 0.0, si = 0.0;
+      if (a.obs_diag) {
+        const double2* E = obs_ops + (int64_t)o * n;
+        for (int i = threadIdx.x; i < n; i += kThreads) {
+          const double2 p = cmul(E[i], rho[(int64_t)i * n + i]);
+          sr += p.x; si += p.y;
+        }
+      } else {
+        const double2* E = obs_ops + o * nn;
+        for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+          const int i = (int)(e / n), j = (int)(e % n);
+          const double2 p = cmul(E[(int64_t)j * n + i], rho[e]);
+          sr += p.x; si += p.y;
+        }
+      }
+      sr = block_sum<kThreads>(sr, red);
+      si = block_sum<kThreads>(si, red);
+      if (threadIdx.x == 0)
+        a.obs_out[((int64_t)b * a.obs_per_inst + oslot) * a.n_obs + o] = make_double2(sr, si);
+    }
+    if (a.trace_tol > 0.0) {
+      double t = 0.0;
+      for (int i = threadIdx.x; i < n; i += kThreads) t += rho[(int64_t)i * n + i].x;
+      t = block_sum<kThreads>(t, red);
+      if (fabs(t - tr0) > a.trace_tol * fmax(1.0, fabs(tr0))) flags |= LIME_FLAG_TRACE_DRIFT;
+    }
+    if (a.states && ((gstep + 1) % a.states_every) == 0) {
+      const int slot = (gstep + 1) / a.states_every - 1;
+      double2* dst = a.states + ((int64_t)b * a.states_per_inst + slot) * nn;
+      for (int64_t e = threadIdx.x; e < nn; e += kThreads) dst[e] = rho[e];
+    }
+  }
+  if (flags) atomicOr(a.status, flags);
+}
+
+// Heff = H - (i/2) sum_k L_k^dag L_k ;  M = sum_k l_k l_k^dag
+__global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
+  const int b = blockIdx.x;
+  const int n = d.n;
+  const int64_t nn = (int64_t)n * n;
+  const double2* H = reinterpret_cast<const double2*>(d.h) + b * d.h_stride;
+  const double2* Ld = d.l_dense ? reinterpret_cast<const double2*>(d.l_dense) + b * d.l_dense_stride : nullptr;
+  const double2* lg = d.l_diag ? reinterpret_cast<const double2*>(d.l_diag) + b * d.l_diag_stride : nullptr;
+  double2* heff = reinterpret_cast<double2*>(d.heff) + b * nn;
+  double2* M = reinterpret_cast<double2*>(d.m) + b * nn;
+  for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    double2 g = cz();  // (sum_k L_k^dag L_k)_ij
+    for (int k = 0; k < d.k_dense; ++k) {
+      const double2* L = Ld + k * nn;
+      for (int q = 0; q < n; ++q) cfma(g, cconj(L[(int64_t)q * n + i]), L[(int64_t)q * n + j]);
+    }
+    double2 mm = cz();
+    for (int k = 0; k < d.k_diag; ++k) {
+      const double2* l = lg + (int64_t)k * n;
+      cfma(mm, l[i], cconj(l[j]));
+      if (i == j) g = cadd(g, make_double2(l[i].x * l[i].x + l[i].y * l[i].y, 0.0));
+    }
+    // H - (i/2) g  =  (H.re + g.im/2, H.im - g.re/2)
+    const double2 h = H[e];
+    heff[e] = make_double2(h.x + 0.5 * g.y, h.y - 0.5 * g.x);
+    M[e] = mm;
+  }
+}
+
+}  // namespace f64
+}  // namespace lime
+
+using namespace lime;
+
+extern "C" int lime_lindblad_prepare_f64(const LimePrepareDesc* d, void* stream) {
+  if (!d || d->n <= 0 || d->batch <= 0 || d->k_dense < 0 || d->k_diag < 0) return LIME_ERR_ARG;
+  if (!d->h || !d->heff || !d->m) return LIME_ERR_ARG;
+  if ((d->k_dense > 0 && !d->l_dense) || (d->k_diag > 0 && !d->l_diag)) return LIME_ERR_ARG;
+  if (d->h_stride < 0 || d->l_dense_stride < 0 || d->l_diag_stride < 0) return LIME_ERR_ARG;
+  f64::prepare_kernel<<<d->batch, f64::kThreads, 0, (cudaStream_t)stream>>>(*d);
+  LIME_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return LIME_OK;
+}
+
+extern "C" size_t lime_lindblad_rk4_f64_workspace(int32_t n, int32_t batch, int32_t k_dense) {
+  if (n <= 0 || batch <= 0 || k_dense < 0) return 0;
+  const size_t mats = (size_t)f64::ws_mats(k_dense) * (size_t)n * n * sizeof(double2);
+  return (size_t)batch * (mats + sizeof(double));
+}
+
+template <int TM>
+static int launch_f64(f64::RK4Args& args, int batch, cudaStream_t st) {
+  const size_t smem = (size_t)(16 * TM) * (f64::kKC + 1) * sizeof(double2) +
+                      (size_t)f64::kKC * (16 * TM + 1) * sizeof(double2);
+  auto kern = f64::lindblad_rk4_f64_kernel<TM>;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<batch, f64::kThreads, smem, st>>>(args);
+  LIME_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return LIME_OK;
+}
+
+extern "C" int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream) {
+  if (!d) return LIME_ERR_ARG;
+  if (d->n <= 0 || d->batch <= 0 || d->n_steps < 0 || d->k_dense < 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (!d->rho || !d->heff || !d->status || !d->workspace) return LIME_ERR_ARG;
+  if (d->k_dense > 0 && !d->l_dense) return LIME_ERR_ARG;
+  if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
+  if (d->states && d->states_every <= 0) return LIME_ERR_ARG;
+  if (d->heff_stride < 0 || d->m_stride < 0 || d->l_dense_stride < 0 || d->obs_stride < 0) return LIME_ERR_ARG;
+  const int pb = d->param_batch > 0 ? d->param_batch : d->batch;
+  if (pb > d->batch) return LIME_ERR_ARG;
+  if (!(d->dt == d->dt)) return LIME_ERR_ARG;
+  if (d->workspace_bytes < lime_lindblad_rk4_f64_workspace(d->n, d->batch, d->k_dense))
+    return LIME_ERR_WORKSPACE;
+  if (d->n_steps == 0) return LIME_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t nn = (int64_t)d->n * d->n;
+  f64::RK4Args a{};
+  a.n = d->n; a.param_batch = pb; a.k_dense = d->k_dense; a.n_obs = d->n_obs; a.obs_diag = d->obs_diag;
+  a.states_every = d->states ? d->states_every : 1;
+  a.states_per_inst = d->states ? d->n_steps / d->states_every : 0;
+  a.dt = d->dt; a.trace_tol = d->trace_tol;
+  a.rho = reinterpret_cast<double2*>(d->rho);
+  a.heff = reinterpret_cast<const double2*>(d->heff); a.heff_stride = d->heff_stride;
+  a.m = reinterpret_cast<const double2*>(d->m); a.m_stride = d->m_stride;
+  a.l_dense = reinterpret_cast<const double2*>(d->l_dense); a.l_dense_stride = d->l_dense_stride;
+  a.obs_ops = reinterpret_cast<const double2*>(d->obs_ops); a.obs_stride = d->obs_stride;
+  a.obs_out = reinterpret_cast<double2*>(d->obs_out);
+  a.obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  a.obs_per_inst = d->n_steps / a.obs_every;
+  a.states = reinterpret_cast<double2*>(d->states);
+  a.ws = reinterpret_cast<double2*>(d->workspace);
+  a.tr0 = reinterpret_cast<double*>(reinterpret_cast<char*>(d->workspace) +
+                                    (size_t)d->batch * f64::ws_mats(d->k_dense) * nn * sizeof(double2));
+  a.status = d->status;
+  // bounded launches: at most ~2^27 complex MACs of GEMM per instance per launch
+  const double per_step = 4.0 * (1 + 2 * d->k_dense) * (double)nn * d->n;
+  int chunk = (int)fmax(1.0, fmin((double)d->n_steps, 134217728.0 / per_step));
+  for (int s0 = 0; s0 < d->n_steps; s0 += chunk) {
+    a.step0 = s0;
+    a.n_steps = (d->n_steps - s0 < chunk) ? d->n_steps - s0 : chunk;
+    int rc;
+    if (d->n <= 16) rc = launch_f64<1>(a, d->batch, st);
+    else if (d->n <= 32) rc = launch_f64<2>(a, d->batch, st);
+    else rc = launch_f64<4>(a, d->batch, st);
+    if (rc != LIME_OK) return rc;
+  }
+  return LIME_OK;
+}
