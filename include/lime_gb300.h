@@ -46,6 +46,8 @@ typedef enum {
   LIME_ERR_CUDA = -3,         /* a CUDA runtime call failed                */
   LIME_ERR_NO_DEVICE = -4,    /* no sm_103 device current                  */
   LIME_ERR_WORKSPACE = -5,    /* workspace too small                       */
+  LIME_ERR_SCRATCH_LIMIT = -6,/* request needs more than the fixed scratch  */
+                              /* of lime_lindblad_rk4_f64_noalloc           */
 } lime_status;
 
 /* bits of the device status word written by kernels */
@@ -119,6 +121,31 @@ typedef struct {
 
 size_t lime_lindblad_rk4_f64_workspace(int32_t n, int32_t batch, int32_t k_dense);
 int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream);
+
+/* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate
+ * device memory: a host framework whose pool owns the GPU, a latency-critical
+ * loop where cudaMalloc/cudaFree would synchronise the device, or a process
+ * that must keep a fixed device footprint after start-up.  No counterpart in
+ * the reference (which has no native code); it has no workspace argument:
+ * d->workspace and d->workspace_bytes are ignored.
+ *   - Scratch is a fixed LIME_NOALLOC_SCRATCH_BYTES array inside the
+ *     library's device image, held on every GPU that loads the library until
+ *     the process exits.  Requests whose workspace
+ *     (lime_lindblad_rk4_f64_workspace) exceeds it return
+ *     LIME_ERR_SCRATCH_LIMIT without launching anything.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress) with that device current; make that first call
+ *     before any stream capture on the device.
+ *   - Nothing is allocated or freed by this call.
+ *   - All calls in the process share one array per device and it keeps the
+ *     previous call's contents; every word a call reads it first writes, but
+ *     calls whose executions overlap on the GPU (different streams, or
+ *     concurrent host threads) race on it and must be serialised by the
+ *     caller.
+ */
+#define LIME_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)
+size_t lime_noalloc_scratch_bytes(void);
+int lime_lindblad_rk4_f64_noalloc(const LimeLindbladDesc* d, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Library info                                                         */

@@ -76,6 +76,8 @@ SIGNATURES = [
     ('lime_lindblad_prepare_f64', c_int32, [ctypes.POINTER(PrepareDesc), c_void_p]),
     ('lime_lindblad_rk4_f64_workspace', c_size_t, [c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_f64', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
+    ('lime_noalloc_scratch_bytes', c_size_t, []),
+    ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_device_check', c_int32, []),
     ('lime_launch_count', c_int64, []),
     ('lime_status_string', ctypes.c_char_p, [c_int32]),

@@ -20,6 +20,8 @@ extern "C" const char* lime_status_string(int status) {
     case LIME_ERR_CUDA: return "CUDA runtime error";
     case LIME_ERR_NO_DEVICE: return "no compute capability 10.3 device is current";
     case LIME_ERR_WORKSPACE: return "workspace too small";
+    case LIME_ERR_SCRATCH_LIMIT:
+      return "request needs more workspace than the no-allocation entry point's fixed scratch";
     default: return "unknown status";
   }
 }
