@@ -148,6 +148,41 @@ size_t lime_noalloc_scratch_bytes(void);
 int lime_lindblad_rk4_f64_noalloc(const LimeLindbladDesc* d, void* stream);
 
 /* ------------------------------------------------------------------ */
+/* Batched split-precision Lindblad RK4 (tensor cores)                  */
+/* ------------------------------------------------------------------ */
+
+/* RK4 propagation of B Hermitian density matrices (n <= 64) on the tcgen05
+ * tensor cores: each stage's Heff * rho is an fp16 hi/lo split product
+ * (three MMAs, fp32 accumulation) of power-of-two pre-scaled operands; the
+ * state is fp32 with an fp32 compensation term; observables, traces and the
+ * final state are produced in FP64.  Replaces the same loops as
+ * lime_lindblad_rk4_f64 (lime/oqs.py:1674-1682, 777-787) for generators
+ * whose collapse operators are site-diagonal projectors or any diagonal
+ * operators with diagonal M (pure dephasing): m_diag[p][i] = M_ii.
+ *   scale_a_log2  A = Heff * 2^scale_a_log2 (choose max|A| ~ 2^12)
+ *   scale_b_log2  B = rho  * 2^scale_b_log2 (choose a bound of |rho_ij| ~ 2^13)
+ *   obs_mode      0 none; 1 populations: obs k = rho_kk (n_obs <= n);
+ *                 2 dense: obs_ops [P|1][n_obs][n][n], Tr(E rho)
+ *   obs_out       [B][n_steps / obs_every][n_obs] complex128
+ *   ctas_per_sm   0 = default (2)
+ * No workspace: state lives on chip for the whole launch.
+ */
+typedef struct {
+  int32_t n, batch, param_batch, n_steps;
+  int32_t obs_mode, n_obs, obs_every;
+  int32_t scale_a_log2, scale_b_log2, ctas_per_sm;
+  double dt, trace_tol;
+  double* rho;
+  const double* heff;     int64_t heff_stride;
+  const double* m_diag;   int64_t m_stride;
+  const double* obs_ops;  int64_t obs_stride;
+  double* obs_out;
+  int32_t* status;
+} LimeLindbladSplitDesc;
+
+int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* Library info                                                         */
 /* ------------------------------------------------------------------ */
 

@@ -70,6 +70,19 @@ class LindbladDesc(ctypes.Structure):
                 ('status', c_void_p)]
 
 
+class SplitDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('batch', c_int32), ('param_batch', c_int32), ('n_steps', c_int32),
+                ('obs_mode', c_int32), ('n_obs', c_int32), ('obs_every', c_int32),
+                ('scale_a_log2', c_int32), ('scale_b_log2', c_int32), ('ctas_per_sm', c_int32),
+                ('dt', c_double), ('trace_tol', c_double),
+                ('rho', c_void_p),
+                ('heff', c_void_p), ('heff_stride', c_int64),
+                ('m_diag', c_void_p), ('m_stride', c_int64),
+                ('obs_ops', c_void_p), ('obs_stride', c_int64),
+                ('obs_out', c_void_p),
+                ('status', c_void_p)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
 SIGNATURES = [
@@ -78,6 +91,7 @@ SIGNATURES = [
     ('lime_lindblad_rk4_f64', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
+    ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),
     ('lime_device_check', c_int32, []),
     ('lime_launch_count', c_int64, []),
     ('lime_status_string', ctypes.c_char_p, [c_int32]),

@@ -220,6 +220,84 @@ def _run_f64(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int,
     return obs_out[:, :, :n_obs], states, status
 
 
+SPLIT_MAX_N = 64
+
+
+def split_supported(gen: LindbladGenerator) -> str | None:
+    """None if the tensor-core path handles ``gen``, else the reason it does not."""
+    if gen.n > SPLIT_MAX_N:
+        return 'dimension %d > %d' % (gen.n, SPLIT_MAX_N)
+    if gen.k_dense:
+        return 'dense (non-diagonal) collapse operators'
+    if gen.m is not None and not is_diagonal(gen.m):
+        return 'diagonal collapse operators with a non-diagonal M = sum_k l_k l_k^dag'
+    return None
+
+
+def _pow2_exponent(target: float, bound: float) -> int:
+    import math
+    if not bound > 0 or not math.isfinite(bound):
+        return 0
+    return int(math.floor(math.log2(target / bound)))
+
+
+def _split_obs(e_ops, n, P, device):
+    """(mode, n_obs, tensor, stride) for the split kernel."""
+    if not e_ops:
+        return 0, 0, None, 0
+    E = [as_device(e, device) for e in e_ops]
+    if all(e.dim() == 2 for e in E) and len(E) <= n:
+        pops = torch.zeros((len(E), n, n), dtype=CDT, device=device)
+        idx = torch.arange(len(E), device=device)
+        pops[idx, idx, idx] = 1
+        if torch.equal(torch.stack(E), pops):
+            return 1, len(E), None, 0
+    per = any(e.dim() == 3 for e in E)
+    if per:
+        Et = torch.stack([e.expand(P, n, n) if e.dim() == 2 else e for e in E], 1).contiguous()
+        return 2, len(E), Et, len(E) * n * n
+    return 2, len(E), torch.stack(E, 0).unsqueeze(0).contiguous(), 0
+
+
+def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
+               obs_every: int, trace_tol: float, param_batch: int, events=None,
+               ctas_per_sm: int = 0):
+    lib = nat.require_device()
+    why = split_supported(gen)
+    if why is not None:
+        raise ValueError('precision="split" does not support this generator: ' + why)
+    B, n = rho.shape[0], gen.n
+    mode, n_obs, Et, obs_stride = _split_obs(e_ops, n, gen.P, rho.device)
+    obs_out = torch.zeros((B, n_steps // obs_every, max(n_obs, 1)), dtype=CDT, device=rho.device)
+    status = torch.zeros(1, dtype=torch.int32, device=rho.device)
+    m_diag = None
+    if gen.m is not None:
+        m_diag = torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous()
+    amax = float(gen.heff.abs().max().item())
+    rbound = float(torch.linalg.matrix_norm(rho).max().item()) * (n ** 0.5)
+    d = nat.SplitDesc()
+    d.n, d.batch, d.param_batch, d.n_steps = n, B, param_batch, n_steps
+    d.obs_mode, d.n_obs, d.obs_every = mode, n_obs, obs_every
+    d.scale_a_log2 = _pow2_exponent(4096.0, amax)
+    d.scale_b_log2 = _pow2_exponent(8192.0, rbound)
+    d.ctas_per_sm = ctas_per_sm
+    d.dt, d.trace_tol = float(dt), float(trace_tol)
+    d.rho = rho.data_ptr()
+    d.heff, d.heff_stride = gen.heff.data_ptr(), (0 if gen.heff.shape[0] == 1 else n * n)
+    if m_diag is not None:
+        d.m_diag, d.m_stride = m_diag.data_ptr(), (0 if m_diag.shape[0] == 1 else n)
+    if Et is not None:
+        d.obs_ops, d.obs_stride = Et.data_ptr(), obs_stride
+    d.obs_out = obs_out.data_ptr()
+    d.status = status.data_ptr()
+    if events is not None:
+        events[0].record()
+    nat.check(lib.lime_lindblad_rk4_split(d, _stream_ptr()), 'lime_lindblad_rk4_split')
+    if events is not None:
+        events[1].record()
+    return obs_out[:, :, :n_obs], None, status
+
+
 def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
               states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
               check: bool = True, obs_every: int = 1, events=None):
@@ -248,18 +326,26 @@ def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             B = gen.P
         else:
             raise ValueError('rho0 batch %d does not match %d generators' % (B, gen.P))
-    obs = prepare_obs(e_ops, n, gen.P, device)
+    obs = prepare_obs(e_ops, n, gen.P, device) if precision == 'fp64' else None
     herm = bool(torch.equal(rho, rho.mH))
     if herm:
         work = rho.clone().contiguous()
     else:
         a, b = hermitian_parts(rho)
         work = torch.cat([a, b], 0).contiguous()
-    if precision != 'fp64':
-        raise ValueError("unknown precision %r" % (precision,))
-    tol = 1e-9 if trace_tol is None else trace_tol
-    o, s, status = _run_f64(gen, work, dt, n_steps, obs, obs_every, states_every, tol,
-                            param_batch=B, events=events)
+    if precision == 'fp64':
+        tol = 1e-9 if trace_tol is None else trace_tol
+        o, s, status = _run_f64(gen, work, dt, n_steps, obs, obs_every, states_every, tol,
+                                param_batch=B, events=events)
+    elif precision == 'split':
+        if states_every:
+            raise ValueError('precision="split" keeps the state on chip; states_every is not '
+                             'supported (use precision="fp64" for rholist output)')
+        tol = 1e-5 if trace_tol is None else trace_tol
+        o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
+                                  param_batch=B, events=events)
+    else:
+        raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
     if check:
         flags = int(status.item())
         if flags:

@@ -66,6 +66,7 @@ def _c_layout(struct_name, fields):
 @pytest.mark.parametrize('cname,pyname', [
     ('LimePrepareDesc', 'PrepareDesc'),
     ('LimeLindbladDesc', 'LindbladDesc'),
+    ('LimeLindbladSplitDesc', 'SplitDesc'),
 ])
 def test_descriptor_layout_matches_c(tmp_path, cname, pyname):
     from lime_gb300 import _native
