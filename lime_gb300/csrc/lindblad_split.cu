@@ -46,21 +46,21 @@ namespace lime {
 namespace split {
 
 constexpr int kN = 64;
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;            // 8 warps: TMEM lane quadrant = warp & 3, column half = warp >> 2
+constexpr int kCols = 32;                // columns of the row component owned by one thread
 constexpr int kXtStride = 68;            // floats per transpose-buffer row (conflict-free float4 rows)
 constexpr uint32_t kTmemCols = 256;      // A0 [0,64) | A1 [64,128) | A2 [128,192) | D [192,256)
 constexpr uint32_t kColA0 = 0, kColA1 = 64, kColA2 = 128, kColD = 192;
 constexpr uint32_t kLBO = 128;           // B operand: K-direction core-matrix stride (bytes)
 constexpr uint32_t kSBO = 2048;          // B operand: N-direction 8-row-group stride (bytes)
 constexpr uint32_t kBopBytes = 16384;    // 64 (N) x 128 (K) fp16
-constexpr float kB0Max = 1023.f;         // |B0| / q_B
 constexpr double kA0Max = 127.0;         // |A0| / q_A
 constexpr float kRowFloor = 8.f;         // smallest row bound used for q_B (scaled units)
 
 struct __align__(1024) Smem {
   uint8_t bop[2][kBopBytes];             // B0 (fixed point), B1 (residual)
-  float xt[128 * kXtStride];             // D transpose buffer
-  float rlo[kN * kThreads];              // compensation of rho, [j][t]
+  float xt[128 * kXtStride];             // D transpose buffer, row r = TMEM lane r
+  float rlo[kN * 128];                   // compensation of rho, [j][r]
   float smax[2][kThreads];               // per-thread max |B| of the last written stage input
   double red[2][kThreads / 32];
   uint64_t mbar;
@@ -69,7 +69,7 @@ struct __align__(1024) Smem {
 
 struct Args {
   int n, batch, param_batch, n_steps, step0, obs_mode, n_obs, obs_every, obs_per_inst;
-  float sb, inv_sab, c_half, c_full, c_sixth, c_sixth_lo;
+  float sb, inv_sab, sab_half, c_half, c_full, c_sixth, c_sixth_lo;
   double sa_d;
   double trace_tol;
   double2* rho;
@@ -81,13 +81,16 @@ struct Args {
   uint32_t max_wait;
 };
 
-__device__ __forceinline__ double block_sum2(double v, double* red, int t) {
+__device__ __forceinline__ double block_sum(double v, double* red, int t) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   __syncthreads();
   if ((t & 31) == 0) red[t >> 5] = v;
   __syncthreads();
-  return red[0] + red[1] + red[2] + red[3];
+  double s = 0.0;
+#pragma unroll
+  for (int w = 0; w < kThreads / 32; ++w) s += red[w];
+  return s;
 }
 
 // A row t of the block matrix, in FP64 (pre-scaling applied by the caller).
@@ -102,6 +105,10 @@ __device__ __forceinline__ double a_elem(const double2* heff, int n, int i, int 
 __device__ __forceinline__ uint32_t pack_half2(__half lo, __half hi) {
   return (uint32_t)__half_as_ushort(lo) | ((uint32_t)__half_as_ushort(hi) << 16);
 }
+__device__ __forceinline__ uint32_t pack_f2h2(float lo, float hi) {
+  const __half2 h = __floats2half2_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
 
 // x = a0 + a1 + a2: a0 on the q grid (|a0| <= 127 q), a1/a2 fp16 residuals.
 __device__ __forceinline__ void split_a(double x, double q, double inv_q, __half& a0, __half& a1, __half& a2) {
@@ -113,34 +120,25 @@ __device__ __forceinline__ void split_a(double x, double q, double inv_q, __half
   a2 = __double2half(r1 - (double)__half2float(a1));
 }
 
-// x = b0 + b1: b0 on the q grid (|b0| <= 1023 q), b1 = fp16(x - b0).
-__device__ __forceinline__ void split_b(float x, float q, float inv_q, __half& b0, __half& b1) {
-  const float k = fminf(fmaxf(rintf(x * inv_q), -kB0Max), kB0Max);
-  const float v0 = k * q;
-  b0 = __float2half_rn(v0);
-  b1 = __float2half_rn(x - v0);
+// Row quantum from a bound m of |B| on the row (scaled units): |x| <= 1.5 m
+// stays within 1023 q for q = 2^(floor(log2(1.5 m)) - 9).  Returns the magic
+// constant 1.5 * 2^23 * q: (x + M) - M rounds x to the nearest multiple of q.
+__device__ __forceinline__ float row_magic(float m) {
+  const int e = ilogbf(fmaxf(1.5f * m, kRowFloor));
+  return ldexpf(1.5f, e + 14);
 }
 
-// Power-of-two quantum for a row whose magnitude bound is m (scaled units):
-// |x| <= 1.5 m fits 1023 q with q = 2^(floor(log2(1.5 m)) - 9).
-__device__ __forceinline__ void row_quantum(float m, float& q, float& inv_q) {
-  const float mm = fmaxf(1.5f * m, kRowFloor);
-  const int e = ilogbf(mm);
-  q = ldexpf(1.f, e - 9);
-  inv_q = ldexpf(1.f, 9 - e);
-}
-
-// Write 8 consecutive B^T values (chunk c of this thread's row segment).
-__device__ __forceinline__ void store_b8(Smem& S, uint32_t off, const float* x, float q, float inv_q, float& mx) {
+// Split 8 consecutive B^T values into b0 (q grid) + b1 (fp16 residual) and store.
+__device__ __forceinline__ void store_b8(Smem& S, uint32_t off, const float* x, float magic, float& mx) {
   uint32_t h0[4], h1[4];
 #pragma unroll
   for (int e = 0; e < 4; ++e) {
-    __half a0, a1, b0, b1;
-    split_b(x[2 * e], q, inv_q, a0, a1);
-    split_b(x[2 * e + 1], q, inv_q, b0, b1);
-    h0[e] = pack_half2(a0, b0);
-    h1[e] = pack_half2(a1, b1);
-    mx = fmaxf(mx, fmaxf(fabsf(x[2 * e]), fabsf(x[2 * e + 1])));
+    const float u = x[2 * e], w = x[2 * e + 1];
+    const float u0 = __fsub_rn(__fadd_rn(u, magic), magic);
+    const float w0 = __fsub_rn(__fadd_rn(w, magic), magic);
+    h0[e] = pack_f2h2(u0, w0);
+    h1[e] = pack_f2h2(__fsub_rn(u, u0), __fsub_rn(w, w0));
+    mx = fmaxf(mx, fmaxf(fabsf(u), fabsf(w)));
   }
   *reinterpret_cast<uint4*>(S.bop[0] + off) = make_uint4(h0[0], h0[1], h0[2], h0[3]);
   *reinterpret_cast<uint4*>(S.bop[1] + off) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
@@ -170,13 +168,32 @@ __device__ __forceinline__ bool mma_pass(uint32_t tbase, uint32_t b0_addr, uint3
   return tc::mbar_wait_bounded(mbar, parity, max_wait);
 }
 
+// Two-sum update of (hi, lo) += (acc + f) dt/6 with dt/6 = c6 + c6lo.
+__device__ __forceinline__ float rk4_final(float x, float accj, float f, float c6, float c6lo, float& lo) {
+  const float ksum = __fadd_rn(accj, f);
+  const float inc = __fmul_rn(ksum, c6);
+  const float inc_res = __fmaf_rn(ksum, c6, -inc);
+  const float inc_lo = __fmaf_rn(ksum, c6lo, inc_res);
+  const float sum = __fadd_rn(x, inc);
+  const float bv = __fsub_rn(sum, x);
+  const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(sum, bv)), __fsub_rn(inc, bv));
+  float l = __fadd_rn(lo, __fadd_rn(err, inc_lo));
+  const float hi2 = __fadd_rn(sum, l);
+  lo = __fsub_rn(l, __fsub_rn(hi2, sum));
+  return hi2;
+}
+
 __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a) {
   extern __shared__ uint8_t smem_raw[];
   Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int t = threadIdx.x, warp = t >> 5;
-  const bool is_re = t >= 64;   // rows 64..127 of D hold Xi and give Re f
-  const int i = t & 63;
-  const int partner = is_re ? i : 64 + i;   // the other component of row i
+  const int lq = warp & 3;                  // TMEM lane quadrant
+  const int h = warp >> 2;                  // column half
+  const int r = lq * 32 + (t & 31);         // row of [Xr; Xi] = TMEM lane (t = 128 h + r)
+  const bool is_re = r >= 64;               // rows 64..127 hold Xi and give Re f
+  const int i = r & 63;
+  const int j0 = kCols * h;
+  const bool diag_owner = is_re && (i >> 5) == h;   // holds the (real) diagonal element rho_ii
   const int n = a.n;
 
   if (warp == 0) {
@@ -191,12 +208,14 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tbase = S.tmem_base;
-  const uint32_t lane_addr = tbase + ((uint32_t)(warp * 32) << 16);
+  const uint32_t lane_addr = tbase + ((uint32_t)(lq * 32) << 16);
   const uint32_t b0_addr = tc::smem_u32(S.bop[0]);
   const uint32_t b1_addr = tc::smem_u32(S.bop[1]);
   const uint32_t brow = (uint32_t)(i >> 3) * kSBO + (uint32_t)(i & 7) * 16u;
-  const uint32_t bchunk0 = is_re ? 0u : 8u;
+  const uint32_t bchunk0 = (is_re ? 0u : 8u) + 4u * (uint32_t)h;
   const float bsign = is_re ? a.sb : -a.sb;
+  float* xrow = S.xt + r * kXtStride;
+  const float* xcol = S.xt + (is_re ? 64 : 0) * kXtStride + i;   // X[j][i] at xcol[j * stride]
   uint32_t phase = 0;
   int flags = 0;
   bool aborted = false;
@@ -207,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
     const double2* heff = a.heff + p * a.heff_stride;
     const float mi = (a.m_diag && i < n) ? (float)a.m_diag[p * a.m_stride + i] : 0.f;
 
-    // ---- A operand: scaled Heff block row t -> TMEM as A0 + A1 + A2 ----
+    // ---- A operand: scaled Heff block row r -> TMEM as A0 + A1 + A2 (this thread: k in [64h, 64h+64)) ----
     {
       double rmax = 0.0;
       for (int k = 0; k < 128; ++k) rmax = fmax(rmax, fabs(a_elem(heff, n, i, k, is_re) * a.sa_d));
@@ -218,11 +237,11 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         inv_q = ldexp(1.0, 6 - e);
       }
 #pragma unroll 1
-      for (int qq = 0; qq < 4; ++qq) {
+      for (int qq = 0; qq < 2; ++qq) {
         uint32_t p0[16], p1[16], p2[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          const int k = qq * 32 + 2 * c;
+          const int k = 64 * h + qq * 32 + 2 * c;
           __half x0, x1, x2, y0, y1, y2;
           split_a(a_elem(heff, n, i, k, is_re) * a.sa_d, q, inv_q, x0, x1, x2);
           split_a(a_elem(heff, n, i, k + 1, is_re) * a.sa_d, q, inv_q, y0, y1, y2);
@@ -230,47 +249,48 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
           p1[c] = pack_half2(x1, y1);
           p2[c] = pack_half2(x2, y2);
         }
-        tc::tmem_st16(lane_addr + kColA0 + qq * 16, p0);
-        tc::tmem_st16(lane_addr + kColA1 + qq * 16, p1);
-        tc::tmem_st16(lane_addr + kColA2 + qq * 16, p2);
+        const uint32_t col = 32 * h + 16 * qq;
+        tc::tmem_st16(lane_addr + kColA0 + col, p0);
+        tc::tmem_st16(lane_addr + kColA1 + col, p1);
+        tc::tmem_st16(lane_addr + kColA2 + col, p2);
       }
       tc::tmem_wait_st();
     }
 
-    // ---- state: this thread's component of row i ----
-    float rho[kN], acc[kN];
+    // ---- state: columns [j0, j0+32) of this thread's row component ----
+    float rho[kCols], acc[kCols];
     const double2* r0 = a.rho + (int64_t)b * n * n;
     double dtr = 0.0;
     float mx = 0.f;
+    float rho_d = 0.f, acc_d = 0.f, rs_d = 0.f;   // diagonal element (diag_owner only)
 #pragma unroll
-    for (int j = 0; j < kN; ++j) {
+    for (int jj = 0; jj < kCols; ++jj) {
+      const int j = j0 + jj;
       double v = 0.0;
       if (i < n && j < n) {
         const double2 z = r0[(int64_t)i * n + j];
         v = is_re ? z.x : z.y;
       }
-      const float h = (float)v;
-      rho[j] = h;
-      S.rlo[j * kThreads + t] = (float)(v - (double)h);
-      mx = fmaxf(mx, fabsf(h * a.sb));
-      if (is_re && j == i) dtr = v;
+      const float hv = (float)v;
+      rho[jj] = hv;
+      S.rlo[j * 128 + r] = (float)(v - (double)hv);
+      mx = fmaxf(mx, fabsf(hv * a.sb));
+      if (diag_owner && j == i) { dtr = v; rho_d = hv; }
     }
+    rs_d = rho_d;
     S.smax[g & 1][t] = mx;
-    const double tr0 = block_sum2(dtr, S.red[0], t);   // (its barriers publish smax)
-    float rs_diag = 0.f;   // Re rho_s[i][i] of the current stage input (RE threads)
-#pragma unroll
-    for (int j = 0; j < kN; ++j)
-      if (j == i) rs_diag = rho[j];
+    const double tr0 = block_sum(dtr, S.red[0], t);   // (its barriers publish smax)
     {
-      float q, inv_q;
-      row_quantum(fmaxf(S.smax[g & 1][t], S.smax[g & 1][partner]), q, inv_q);
+      const float m4 = fmaxf(fmaxf(S.smax[g & 1][i], S.smax[g & 1][64 + i]),
+                             fmaxf(S.smax[g & 1][128 + i], S.smax[g & 1][192 + i]));
+      const float magic = row_magic(m4);
       float dummy = 0.f;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
+      for (int c = 0; c < 4; ++c) {
         float x[8];
 #pragma unroll
         for (int e = 0; e < 8; ++e) x[e] = rho[8 * c + e] * bsign;
-        store_b8(S, brow + (bchunk0 + c) * kLBO, x, q, inv_q, dummy);
+        store_b8(S, brow + (bchunk0 + c) * kLBO, x, magic, dummy);
       }
     }
 
@@ -290,14 +310,13 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
           break;
         }
         tc::tc_fence_after();
-        float* xrow = S.xt + t * kXtStride;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 2; ++q) {
           float v[16];
-          tc::tmem_ld16(lane_addr + kColD + q * 16, v);
+          tc::tmem_ld16(lane_addr + kColD + j0 + q * 16, v);
 #pragma unroll
           for (int e = 0; e < 4; ++e)
-            *reinterpret_cast<float4*>(xrow + q * 16 + 4 * e) =
+            *reinterpret_cast<float4*>(xrow + j0 + q * 16 + 4 * e) =
                 make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
         }
         // ---- pass 2: the exact product A0.B0 into D ----
@@ -311,82 +330,78 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         }
         tc::tc_fence_after();
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 2; ++q) {
           float v[16];
-          tc::tmem_ld16(lane_addr + kColD + q * 16, v);
+          tc::tmem_ld16(lane_addr + kColD + j0 + q * 16, v);
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            float4* p4 = reinterpret_cast<float4*>(xrow + q * 16 + 4 * e);
+            float4* p4 = reinterpret_cast<float4*>(xrow + j0 + q * 16 + 4 * e);
             const float4 o = *p4;
             *p4 = make_float4(__fadd_rn(v[4 * e], o.x), __fadd_rn(v[4 * e + 1], o.y),
                               __fadd_rn(v[4 * e + 2], o.z), __fadd_rn(v[4 * e + 3], o.w));
           }
         }
-        // the quantum for the next B operand (from this stage input's row bound)
-        float qb, inv_qb;
-        row_quantum(fmaxf(S.smax[g & 1][t], S.smax[g & 1][partner]), qb, inv_qb);
+        // dephasing jump term m_i rho_ii folded into the diagonal of X (it
+        // enters Re f_ii = (X_ii + X_ii) / (sa sb) twice, hence the half)
+        if (diag_owner) xrow[i] = __fmaf_rn(mi * a.sab_half, rs_d, xrow[i]);
+        const float m4 = fmaxf(fmaxf(S.smax[g & 1][i], S.smax[g & 1][64 + i]),
+                               fmaxf(S.smax[g & 1][128 + i], S.smax[g & 1][192 + i]));
+        const float magic = row_magic(m4);
         __syncthreads();
 
-        const float* xcol = S.xt + (is_re ? 64 : 0) * kXtStride + i;   // X[j][i] at xcol[j * stride]
         const float cst = (s == 2) ? a.c_full : a.c_half;
-        const float w = (s == 0 || s == 3) ? 1.f : 2.f;
-        float rs_diag_next = rs_diag;
         float nmx = 0.f;
+        // diagonal element, with exactly the operations the loop applies to it
+        float rs_d_next = rs_d;
+        float lo_d = 0.f;
+        if (diag_owner) {
+          const float xd = xrow[i];
+          const float fd = __fmul_rn(__fadd_rn(xd, xd), a.inv_sab);
+          if (s == 0) acc_d = fd;
+          else if (s < 3) acc_d = __fmaf_rn(2.f, fd, acc_d);
+          if (s < 3) {
+            rs_d_next = __fmaf_rn(cst, fd, rho_d);
+          } else {
+            lo_d = S.rlo[i * 128 + r];
+            rho_d = rk4_final(rho_d, acc_d, fd, a.c_sixth, a.c_sixth_lo, lo_d);
+            rs_d_next = rho_d;
+          }
+        }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < 2; ++q) {
           float own[16];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const float4 o = *reinterpret_cast<const float4*>(xrow + q * 16 + 4 * e);
+            const float4 o = *reinterpret_cast<const float4*>(xrow + j0 + q * 16 + 4 * e);
             own[4 * e] = o.x; own[4 * e + 1] = o.y; own[4 * e + 2] = o.z; own[4 * e + 3] = o.w;
           }
           float nxt[16];
 #pragma unroll
           for (int e = 0; e < 16; ++e) {
-            const int j = q * 16 + e;
-            const float tr = xcol[j * kXtStride];
-            float f = (is_re ? (own[e] + tr) : (tr - own[e])) * a.inv_sab;
-            if (is_re && j == i) f = __fmaf_rn(mi, rs_diag, f);
-            if (s == 0) {
-              acc[j] = f;
-            } else if (s < 3) {
-              acc[j] = __fmaf_rn(w, f, acc[j]);
-            }
+            const int jj = q * 16 + e;
+            const float tr = xcol[(j0 + jj) * kXtStride];
+            const float f = __fmul_rn(is_re ? __fadd_rn(own[e], tr) : __fsub_rn(tr, own[e]), a.inv_sab);
+            if (s == 0) acc[jj] = f;
+            else if (s < 3) acc[jj] = __fmaf_rn(2.f, f, acc[jj]);
             if (s < 3) {
-              nxt[e] = __fmaf_rn(cst, f, rho[j]);
+              nxt[e] = __fmaf_rn(cst, f, rho[jj]);
             } else {
-              // increment (k1 + 2k2 + 2k3 + k4) dt/6 with dt/6 carried as a
-              // float pair and the product's rounding residual kept: a plain
-              // fp32 dt/6 rescales time by up to 2^-24
-              const float ksum = __fadd_rn(acc[j], f);
-              const float inc = __fmul_rn(ksum, a.c_sixth);
-              const float inc_res = __fmaf_rn(ksum, a.c_sixth, -inc);
-              const float inc_lo = __fmaf_rn(ksum, a.c_sixth_lo, inc_res);
-              // two-sum of rho_hi + inc, errors folded into the compensation term
-              const float x = rho[j];
-              const float sum = __fadd_rn(x, inc);
-              const float bv = __fsub_rn(sum, x);
-              const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(sum, bv)), __fsub_rn(inc, bv));
-              float lo = __fadd_rn(S.rlo[j * kThreads + t], __fadd_rn(err, inc_lo));
-              const float hi2 = __fadd_rn(sum, lo);
-              lo = __fsub_rn(lo, __fsub_rn(hi2, sum));
-              rho[j] = hi2;
-              S.rlo[j * kThreads + t] = lo;
-              nxt[e] = hi2;
+              float lo = S.rlo[(j0 + jj) * 128 + r];
+              rho[jj] = rk4_final(rho[jj], acc[jj], f, a.c_sixth, a.c_sixth_lo, lo);
+              S.rlo[(j0 + jj) * 128 + r] = lo;
+              nxt[e] = rho[jj];
             }
-            if (j == i) rs_diag_next = nxt[e];
           }
-          // next B operand: two 8-wide chunks
 #pragma unroll
           for (int h8 = 0; h8 < 2; ++h8) {
             float x[8];
 #pragma unroll
             for (int e = 0; e < 8; ++e) x[e] = nxt[8 * h8 + e] * bsign;
-            store_b8(S, brow + (bchunk0 + 2 * q + h8) * kLBO, x, qb, inv_qb, nmx);
+            store_b8(S, brow + (bchunk0 + 2 * q + h8) * kLBO, x, magic, nmx);
           }
         }
         S.smax[(g + 1) & 1][t] = nmx;
-        rs_diag = rs_diag_next;
+        rs_d = rs_d_next;
       }
       if (aborted) break;
 
@@ -395,9 +410,9 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       if (((gstep + 1) % a.obs_every) == 0) {
         const int slot = (gstep + 1) / a.obs_every - 1;
         double2* orow = a.obs_out + ((int64_t)b * a.obs_per_inst + slot) * a.n_obs;
+        const double dval = diag_owner ? (double)rho_d + (double)S.rlo[i * 128 + r] : 0.0;
         if (a.obs_mode == 1) {
-          if (is_re && i < a.n_obs)
-            orow[i] = make_double2((double)rs_diag + (double)S.rlo[i * kThreads + t], 0.0);
+          if (diag_owner && i < a.n_obs) orow[i] = make_double2(dval, 0.0);
         } else if (a.obs_mode == 2) {
           const double2* E0 = a.obs_ops + p * a.obs_stride;
           for (int o = 0; o < a.n_obs; ++o) {
@@ -405,28 +420,28 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
             float pr = 0.f, pi = 0.f;
             if (i < n) {
 #pragma unroll
-              for (int j = 0; j < kN; ++j) {
+              for (int jj = 0; jj < kCols; ++jj) {
+                const int j = j0 + jj;
                 if (j < n) {
-                  const double2 e = E[(int64_t)j * n + i];   // E[j][i]
-                  const float er = (float)e.x, ei = (float)e.y;
+                  const double2 ev = E[(int64_t)j * n + i];   // E[j][i]
+                  const float er = (float)ev.x, ei = (float)ev.y;
                   if (is_re) {
-                    pr = __fmaf_rn(er, rho[j], pr);
-                    pi = __fmaf_rn(ei, rho[j], pi);
+                    pr = __fmaf_rn(er, rho[jj], pr);
+                    pi = __fmaf_rn(ei, rho[jj], pi);
                   } else {
-                    pr = __fmaf_rn(-ei, rho[j], pr);
-                    pi = __fmaf_rn(er, rho[j], pi);
+                    pr = __fmaf_rn(-ei, rho[jj], pr);
+                    pi = __fmaf_rn(er, rho[jj], pi);
                   }
                 }
               }
             }
-            const double sr = block_sum2((double)pr, S.red[0], t);
-            const double si = block_sum2((double)pi, S.red[1], t);
+            const double sr = block_sum((double)pr, S.red[0], t);
+            const double si = block_sum((double)pi, S.red[1], t);
             if (t == 0) orow[o] = make_double2(sr, si);
           }
         }
         if (a.trace_tol > 0.0) {
-          const double d = (is_re && i < n) ? (double)rs_diag + (double)S.rlo[i * kThreads + t] : 0.0;
-          const double tr = block_sum2(d, S.red[0], t);
+          const double tr = block_sum((diag_owner && i < n) ? dval : 0.0, S.red[0], t);
           if (fabs(tr - tr0) > a.trace_tol * fmax(1.0, fabs(tr0))) flags |= LIME_FLAG_TRACE_DRIFT;
         }
       }
@@ -437,9 +452,10 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
     if (i < n) {
       double* out = reinterpret_cast<double*>(a.rho + (int64_t)b * n * n);
 #pragma unroll
-      for (int j = 0; j < kN; ++j) {
+      for (int jj = 0; jj < kCols; ++jj) {
+        const int j = j0 + jj;
         if (j < n) {
-          const double v = (double)rho[j] + (double)S.rlo[j * kThreads + t];
+          const double v = (double)rho[jj] + (double)S.rlo[j * 128 + r];
           if (!isfinite(v)) flags |= LIME_FLAG_NONFINITE;
           out[2 * ((int64_t)i * n + j) + (is_re ? 0 : 1)] = v;
         }
@@ -499,6 +515,7 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   a.sa_d = ldexp(1.0, d->scale_a_log2);
   a.sb = ldexpf(1.f, d->scale_b_log2);
   a.inv_sab = ldexpf(1.f, -(d->scale_a_log2 + d->scale_b_log2));
+  a.sab_half = ldexpf(1.f, d->scale_a_log2 + d->scale_b_log2 - 1);
   a.c_half = (float)(d->dt / 2.0);
   a.c_full = (float)d->dt;
   a.c_sixth = (float)(d->dt / 6.0);
