@@ -122,6 +122,50 @@ typedef struct {
 size_t lime_lindblad_rk4_f64_workspace(int32_t n, int32_t batch, int32_t k_dense);
 int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream);
 
+/* ------------------------------------------------------------------ */
+/* Discrete adjoint (gradients) of the FP64 Lindblad RK4 path           */
+/* ------------------------------------------------------------------ */
+
+/* Backpropagates one checkpoint segment of steps [step0, step0 + seg_steps)
+ * through the RK4 steps of lime_lindblad_rk4_f64 (no counterpart in the
+ * reference, which has no gradients).  Per instance (one CTA):
+ *   1. recompute rho_{step0..step0+seg_steps-1} from the checkpoint
+ *      ckpt = rho_{step0};
+ *   2. walking the steps backwards, add the observable source
+ *      Herm(g E^dag) for every observable recorded after the step
+ *      (obs_grad[B][total_steps/obs_every][n_obs] = dL/d conj(obs), torch's
+ *      complex-gradient convention), recompute the stage states and apply
+ *      the exact adjoint of the RK4 step with the adjoint generator
+ *      L^dag(x) = -i(Ga x - x Ga^dag) + Madj o x + sum_k Ladj_k x Ladj_k^dag
+ *      (Ga = -Heff^dag, Madj = conj(M), Ladj_k = L_k^dag);
+ *   3. accumulate dL/dH_kk (grad_diag[B][n]), dL/dH_{k,k+1} for a real
+ *      symmetric bond (grad_bond[B][n-1]) and dL/dgamma_k for dephasing
+ *      operators sqrt(gamma_k)|k><k| (grad_gamma[B][n]) over the stages.
+ * lam [B][n][n]: in, the adjoint state at step0 + seg_steps; out, at step0.
+ */
+typedef struct {
+  int32_t n, batch, param_batch, seg_steps, step0, total_steps;
+  int32_t k_dense, n_obs, obs_diag, obs_every;
+  double dt;
+  const double* ckpt;
+  double* lam;
+  const double* heff;       int64_t heff_stride;
+  const double* m;          int64_t m_stride;
+  const double* l_dense;    int64_t l_dense_stride;
+  const double* heff_adj;   int64_t heff_adj_stride;
+  const double* m_adj;      int64_t m_adj_stride;
+  const double* l_dense_adj; int64_t l_dense_adj_stride;
+  const double* obs_ops;    int64_t obs_stride;
+  const double* obs_grad;
+  double* grad_diag;
+  double* grad_bond;
+  double* grad_gamma;
+  void* workspace;          size_t workspace_bytes;
+} LimeAdjointDesc;
+
+size_t lime_lindblad_adjoint_f64_workspace(int32_t n, int32_t batch, int32_t seg_steps, int32_t k_dense);
+int lime_lindblad_adjoint_f64(const LimeAdjointDesc* d, void* stream);
+
 /* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate
  * device memory: a host framework whose pool owns the GPU, a latency-critical
  * loop where cudaMalloc/cudaFree would synchronise the device, or a process

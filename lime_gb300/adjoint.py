@@ -1,0 +1,158 @@
+"""Gradients of Lindblad observables through the discrete RK4 adjoint.
+
+``chain_observables`` propagates density matrices of a Frenkel-chain model
+
+    H = H0 + sum_k eps_k |s_k><s_k| + sum_k J_k (|s_k><s_{k+1}| + h.c.)
+    c_ops = { sqrt(gamma_k) |s_k><s_k| }_k          (s_k = site0 + k)
+
+with the FP64 RK4 propagator (the time loop of ``_lindblad``,
+lime/oqs.py:1590-1688) and returns the observables ``Tr(E rho(t))`` as a
+differentiable torch tensor.  Its backward pass runs the hand-written
+adjoint kernel (``lime_lindblad_adjoint_f64``): states are checkpointed every
+``checkpoint`` steps in the forward pass and recomputed segment by segment,
+and the gradients with respect to every site energy, bond coupling and
+dephasing rate are accumulated in FP64 on the device.
+
+Non-Hermitian starting states (the dipole correlation <mu(t) mu(0)> starts
+from mu|g><g|) run as their two Hermitian parts rho = A + iB; for complex
+observables torch's convention dL = Re sum conj(grad) d(obs) makes the
+source of the B chain ``-i grad``.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _native as nat
+from . import engine
+
+CDT = torch.complex128
+
+
+def chain_hamiltonian(H0: torch.Tensor, eps: torch.Tensor, bond: torch.Tensor, site0: int) -> torch.Tensor:
+    """H0 (B|1, N, N) + diag(eps) + bonds on sites site0..site0+n_sites-1."""
+    B, ns = eps.shape
+    N = H0.shape[-1]
+    H = H0.expand(B, N, N).clone().to(CDT)
+    idx = torch.arange(ns, device=H.device) + site0
+    H[:, idx, idx] += eps.to(CDT)
+    if ns > 1:
+        H[:, idx[:-1], idx[1:]] += bond.to(CDT)
+        H[:, idx[1:], idx[:-1]] += bond.to(CDT)
+    return H
+
+
+def dephasing_diagonals(gamma: torch.Tensor, N: int, site0: int) -> torch.Tensor:
+    """l (B, n_sites, N) with l[b, k, site0+k] = sqrt(gamma[b, k])."""
+    B, ns = gamma.shape
+    l = torch.zeros((B, ns, N), dtype=CDT, device=gamma.device)
+    k = torch.arange(ns, device=gamma.device)
+    l[:, k, k + site0] = torch.sqrt(gamma).to(CDT)
+    return l
+
+
+class _ChainObservables(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, eps, bond, gamma, H0, rho0, E, dt, n_steps, site0, obs_every, checkpoint):
+        dev = eps.device
+        B, ns = eps.shape
+        N = H0.shape[-1]
+        H = chain_hamiltonian(H0, eps.detach(), bond.detach(), site0)
+        l = dephasing_diagonals(gamma.detach(), N, site0)
+        gen = engine.LindbladGenerator.build(H, [engine.DiagonalOps(l)], device=dev)
+        rho = rho0.to(device=dev, dtype=CDT)
+        if rho.dim() == 2:
+            rho = rho.unsqueeze(0).expand(B, N, N)
+        herm = bool(torch.equal(rho, rho.mH))
+        if herm:
+            work = rho.clone().contiguous()
+        else:
+            a, b = engine.hermitian_parts(rho)
+            work = torch.cat([a, b], 0).contiguous()
+        ckpt0 = work.clone()
+        obs = engine.prepare_obs(list(E), N, B, dev)
+        K = max(1, min(checkpoint, n_steps))
+        o, states, status = engine._run_f64(gen, work, dt, n_steps, obs, obs_every, K, 0.0,
+                                            param_batch=B)
+        flags = int(status.item())
+        if flags:
+            raise nat.KernelFlagError(flags, 'chain_observables forward')
+        if not herm:
+            o_out = o[:B] + 1j * o[B:]
+        else:
+            o_out = o
+        ctx.save_for_backward(gen.heff, gen.m, ckpt0, states, obs[0])
+        ctx.meta = (B, N, ns, herm, dt, n_steps, site0, obs_every, K, obs[1], obs[2], obs[3])
+        return o_out.clone()
+
+    @staticmethod
+    def backward(ctx, g):
+        heff, m, ckpt0, states, Et = ctx.saved_tensors
+        B, N, ns, herm, dt, n_steps, site0, obs_every, K, n_obs, obs_diag, obs_stride = ctx.meta
+        lib = nat.require_device()
+        dev = heff.device
+        g = g.to(CDT).contiguous()
+        gsrc = g if herm else torch.cat([g, -1j * g], 0).contiguous()
+        C = gsrc.shape[0]                       # number of Hermitian chains x B
+        heff_adj = (-heff.mH).contiguous()
+        m_adj = None if m is None else m.conj().contiguous()
+        lam = torch.zeros((C, N, N), dtype=CDT, device=dev)
+        gd = torch.zeros((C, N), dtype=torch.float64, device=dev)
+        gb = torch.zeros((C, max(N - 1, 1)), dtype=torch.float64, device=dev)
+        gg = torch.zeros((C, N), dtype=torch.float64, device=dev)
+        n_seg = (n_steps + K - 1) // K
+        wsb = lib.lime_lindblad_adjoint_f64_workspace(N, C, K, 0)
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        for sgi in range(n_seg - 1, -1, -1):
+            s0 = sgi * K
+            seg = min(K, n_steps - s0)
+            ck = ckpt0 if sgi == 0 else states[:, sgi - 1].contiguous()
+            d = nat.AdjointDesc()
+            d.n, d.batch, d.param_batch, d.seg_steps = N, C, B, seg
+            d.step0, d.total_steps = s0, n_steps
+            d.k_dense, d.n_obs, d.obs_diag, d.obs_every = 0, n_obs, obs_diag, obs_every
+            d.dt = float(dt)
+            d.ckpt, d.lam = ck.data_ptr(), lam.data_ptr()
+            d.heff, d.heff_stride = heff.data_ptr(), (0 if heff.shape[0] == 1 else N * N)
+            d.heff_adj, d.heff_adj_stride = heff_adj.data_ptr(), (0 if heff.shape[0] == 1 else N * N)
+            if m is not None:
+                d.m, d.m_stride = m.data_ptr(), (0 if m.shape[0] == 1 else N * N)
+                d.m_adj, d.m_adj_stride = m_adj.data_ptr(), (0 if m.shape[0] == 1 else N * N)
+            if n_obs > 0:
+                d.obs_ops, d.obs_stride = Et.data_ptr(), obs_stride
+                d.obs_grad = gsrc.data_ptr()
+            d.grad_diag, d.grad_bond, d.grad_gamma = gd.data_ptr(), gb.data_ptr(), gg.data_ptr()
+            d.workspace, d.workspace_bytes = ws.data_ptr(), wsb
+            nat.check(lib.lime_lindblad_adjoint_f64(d, torch.cuda.current_stream().cuda_stream),
+                      'lime_lindblad_adjoint_f64')
+        if not herm:
+            gd = gd[:B] + gd[B:]
+            gb = gb[:B] + gb[B:]
+            gg = gg[:B] + gg[B:]
+        sl = slice(site0, site0 + ns)
+        g_eps = gd[:, sl]
+        g_bond = gb[:, site0:site0 + ns - 1] if ns > 1 else gb[:, :0]
+        g_gamma = gg[:, sl]
+        return g_eps, g_bond, g_gamma, None, None, None, None, None, None, None, None
+
+
+def chain_observables(H0, eps, bond, gamma, rho0, e_ops, dt: float, n_steps: int, site0: int = 0,
+                      obs_every: int = 1, checkpoint: int = 64, precision: str = 'fp64'):
+    """Observables Tr(E rho) of the chain model, differentiable in eps, bond, gamma.
+
+    ``eps`` (B, n_sites), ``bond`` (B, n_sites - 1), ``gamma`` (B, n_sites)
+    are real tensors on the GPU; ``H0`` (N, N) or (B, N, N) holds the rest of
+    the Hamiltonian (e.g. the ground state of an absorption model);
+    ``rho0`` (N, N) or (B, N, N); ``e_ops`` a list of (N, N) observables.
+    Returns (B, n_steps // obs_every, n_obs) complex128 with observable k
+    recorded after step (k + 1) obs_every - 1.
+    """
+    if precision != 'fp64':
+        raise ValueError('chain_observables differentiates the FP64 path (precision="fp64")')
+    dev = eps.device
+    H0 = engine.as_device(H0, dev)
+    if H0.dim() == 2:
+        H0 = H0.unsqueeze(0)
+    rho0 = engine.as_device(rho0, dev)
+    E = [engine.as_device(e, dev) for e in e_ops]
+    return _ChainObservables.apply(eps, bond, gamma, H0, rho0, E, float(dt), int(n_steps), int(site0),
+                                   int(obs_every), int(checkpoint))

@@ -215,6 +215,211 @@ __global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
   if (flags) atomicOr(a.status, flags);
 }
 
+// ---------------------------------------------------------------- adjoint
+// One generator in the Hermitian form f = -i(G x - x G^dag) + M o x + sum_k L_k x L_k^dag.
+struct Gen {
+  const double2* g;
+  const double2* m;   // may be null
+  const double2* l;   // k dense operators, may be null
+  int k;
+};
+
+// out = gen(x); X, Y, J are n x n scratch.  Whole CTA; ends synchronised.
+template <int TM>
+__device__ void apply_gen(const Gen& G, const double2* x, double2* out, double2* X, double2* Y, double2* J, int n,
+                          double2* smem) {
+  const int64_t nn = (int64_t)n * n;
+  cta_cgemm<TM>(G.g, x, false, X, false, n, smem);
+  for (int k = 0; k < G.k; ++k) {
+    const double2* L = G.l + k * nn;
+    cta_cgemm<TM>(L, x, false, Y, false, n, smem);
+    cta_cgemm<TM>(Y, L, true, J, k > 0, n, smem);
+  }
+  for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+    const int i = (int)(e / n), j = (int)(e % n);
+    const double2 a = X[e], b = X[(int64_t)j * n + i];
+    double2 f = make_double2(a.y + b.y, b.x - a.x);   // -i (X - X^dag)
+    if (G.m) f = cadd(f, cmul(G.m[e], x[e]));
+    if (G.k > 0) f = cadd(f, J[e]);
+    out[e] = f;
+  }
+  __syncthreads();
+}
+
+struct AdjArgs {
+  int n, param_batch, seg_steps, step0, total_steps, k_dense, n_obs, obs_diag, obs_every, obs_per_inst;
+  double dt;
+  const double2* ckpt;
+  double2* lam;
+  const double2* heff; int64_t heff_stride;
+  const double2* m; int64_t m_stride;
+  const double2* ld; int64_t ld_stride;
+  const double2* heff_adj; int64_t heff_adj_stride;
+  const double2* m_adj; int64_t m_adj_stride;
+  const double2* ld_adj; int64_t ld_adj_stride;
+  const double2* obs_ops; int64_t obs_stride;
+  const double2* obs_grad;
+  double* g_diag;
+  double* g_bond;
+  double* g_gamma;
+  double2* ws;
+};
+
+__host__ __device__ inline int64_t adj_ws_mats(int seg_steps, int k_dense) {
+  return (int64_t)seg_steps + 9 + (k_dense > 0 ? 2 : 0);
+}
+
+// Parameter-gradient contributions of one stage: abar = adjoint of the stage
+// derivative, y = stage state (both Hermitian).  Thread-strided over rows.
+__device__ void grad_terms(const double2* abar, const double2* y, int n, double* gd, double* gb, double* gg) {
+  for (int k = threadIdx.x; k < n; k += kThreads) {
+    double sd = 0.0, sg = 0.0, sb = 0.0;
+    for (int x = 0; x < n; ++x) {
+      const double2 a = abar[(int64_t)k * n + x], v = y[(int64_t)k * n + x];
+      sd += a.x * v.y - a.y * v.x;                 // Im(conj(a) y)
+      if (x != k) sg -= a.x * v.x + a.y * v.y;      // -Re(conj(a) y), off-diagonal
+      if (k + 1 < n) {
+        const double2 a2 = abar[(int64_t)(k + 1) * n + x], v2 = y[(int64_t)(k + 1) * n + x];
+        sb += (a.x * v2.y - a.y * v2.x) + (a2.x * v.y - a2.y * v.x);
+      }
+    }
+    gd[k] += 2.0 * sd;
+    gg[k] += sg;
+    if (k + 1 < n) gb[k] += 2.0 * sb;
+  }
+}
+
+template <int TM>
+__global__ void __launch_bounds__(kThreads) lindblad_adjoint_f64_kernel(AdjArgs a) {
+  extern __shared__ double2 smem[];
+  const int b = blockIdx.x;
+  const int n = a.n;
+  const int64_t nn = (int64_t)n * n;
+  const int p = b % a.param_batch;
+  const Gen F{a.heff + p * a.heff_stride, a.m ? a.m + p * a.m_stride : nullptr,
+              a.ld ? a.ld + p * a.ld_stride : nullptr, a.k_dense};
+  const Gen A{a.heff_adj + p * a.heff_adj_stride, a.m_adj ? a.m_adj + p * a.m_adj_stride : nullptr,
+              a.ld_adj ? a.ld_adj + p * a.ld_adj_stride : nullptr, a.k_dense};
+  double2* ws = a.ws + (int64_t)b * adj_ws_mats(a.seg_steps, a.k_dense) * nn;
+  double2* seg = ws;                              // rho_{step0 + s}, s < seg_steps
+  double2* y2 = ws + (int64_t)a.seg_steps * nn;
+  double2* y3 = y2 + nn;
+  double2* y4 = y3 + nn;
+  double2* kk = y4 + nn;
+  double2* ab = kk + nn;
+  double2* yb = ab + nn;
+  double2* lnew = yb + nn;
+  double2* X = lnew + nn;
+  double2* lam_s = X + nn;
+  double2* Y = lam_s + nn;
+  double2* J = Y + nn;
+  double2* lam = a.lam + (int64_t)b * nn;
+  const double2* obs_ops = a.obs_ops ? a.obs_ops + p * a.obs_stride : nullptr;
+  const double dt = a.dt, dt2 = a.dt / 2.0;
+
+  // ---- forward recompute of the segment from its checkpoint ----
+  for (int64_t e = threadIdx.x; e < nn; e += kThreads) seg[e] = a.ckpt[(int64_t)b * nn + e];
+  __syncthreads();
+  for (int s = 0; s + 1 < a.seg_steps; ++s) {
+    const double2* r = seg + (int64_t)s * nn;
+    double2* nxt = seg + (int64_t)(s + 1) * nn;
+    // nxt accumulates k1 + 2k2 + 2k3 + k4 ; y2 holds the current stage input
+    apply_gen<TM>(F, r, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) { nxt[e] = kk[e]; y2[e] = cadd(r[e], cscale(kk[e], dt2)); }
+    __syncthreads();
+    apply_gen<TM>(F, y2, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) { nxt[e] = cadd(nxt[e], cscale(kk[e], 2.0)); y2[e] = cadd(r[e], cscale(kk[e], dt2)); }
+    __syncthreads();
+    apply_gen<TM>(F, y2, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) { nxt[e] = cadd(nxt[e], cscale(kk[e], 2.0)); y2[e] = cadd(r[e], cscale(kk[e], dt)); }
+    __syncthreads();
+    apply_gen<TM>(F, y2, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+      const double2 sum = cadd(nxt[e], kk[e]);
+      nxt[e] = cadd(r[e], cscale(make_double2(sum.x / 6., sum.y / 6.), dt));
+    }
+    __syncthreads();
+  }
+
+  // ---- backward through the segment ----
+  double* GD = a.g_diag + (int64_t)b * n;
+  double* GB = a.g_bond + (int64_t)b * (n > 1 ? n - 1 : 1);
+  double* GG = a.g_gamma + (int64_t)b * n;
+  for (int s = a.seg_steps - 1; s >= 0; --s) {
+    const int gstep = a.step0 + s;   // the step rho_{gstep} -> rho_{gstep+1}
+    // source: observable recorded after this step, Tr(E rho_{gstep+1})
+    if (a.n_obs > 0 && ((gstep + 1) % a.obs_every) == 0) {
+      const int slot = (gstep + 1) / a.obs_every - 1;
+      const double2* gr = a.obs_grad + ((int64_t)b * a.obs_per_inst + slot) * a.n_obs;
+      for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        double2 add = cz();
+        for (int o = 0; o < a.n_obs; ++o) {
+          // Hermitian part of g E^dag: (g conj(E_ji) + conj(g) E_ij) / 2
+          double2 eji, eij;
+          if (a.obs_diag) {
+            const double2 d = (i == j) ? obs_ops[(int64_t)o * n + i] : cz();
+            eji = d; eij = d;
+          } else {
+            eji = obs_ops[o * nn + (int64_t)j * n + i];
+            eij = obs_ops[o * nn + (int64_t)i * n + j];
+          }
+          const double2 g = gr[o];
+          add = cadd(add, cscale(cadd(cmul(g, cconj(eji)), cmul(cconj(g), eij)), 0.5));
+        }
+        lam[e] = cadd(lam[e], add);
+      }
+      __syncthreads();
+    }
+    const double2* r = seg + (int64_t)s * nn;
+    // stage states y2, y3, y4 (y1 = r)
+    apply_gen<TM>(F, r, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) y2[e] = cadd(r[e], cscale(kk[e], dt2));
+    __syncthreads();
+    apply_gen<TM>(F, y2, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) y3[e] = cadd(r[e], cscale(kk[e], dt2));
+    __syncthreads();
+    apply_gen<TM>(F, y3, kk, X, Y, J, n, smem);
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) y4[e] = cadd(r[e], cscale(kk[e], dt));
+    __syncthreads();
+    // adjoint stages
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+      lam_s[e] = lam[e];
+      ab[e] = cscale(lam[e], dt / 6.0);
+    }
+    __syncthreads();
+    apply_gen<TM>(A, ab, yb, X, Y, J, n, smem);                   // ybar4
+    grad_terms(ab, y4, n, GD, GB, GG);
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+      lnew[e] = cadd(lam_s[e], yb[e]);
+      ab[e] = cadd(cscale(lam_s[e], dt / 3.0), cscale(yb[e], dt));
+    }
+    __syncthreads();
+    apply_gen<TM>(A, ab, yb, X, Y, J, n, smem);                   // ybar3
+    grad_terms(ab, y3, n, GD, GB, GG);
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+      lnew[e] = cadd(lnew[e], yb[e]);
+      ab[e] = cadd(cscale(lam_s[e], dt / 3.0), cscale(yb[e], dt2));
+    }
+    __syncthreads();
+    apply_gen<TM>(A, ab, yb, X, Y, J, n, smem);                   // ybar2
+    grad_terms(ab, y2, n, GD, GB, GG);
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+      lnew[e] = cadd(lnew[e], yb[e]);
+      ab[e] = cadd(cscale(lam_s[e], dt / 6.0), cscale(yb[e], dt2));
+    }
+    __syncthreads();
+    apply_gen<TM>(A, ab, yb, X, Y, J, n, smem);                   // ybar1
+    grad_terms(ab, r, n, GD, GB, GG);
+    __syncthreads();
+    for (int64_t e = threadIdx.x; e < nn; e += kThreads) lam[e] = cadd(lnew[e], yb[e]);
+    __syncthreads();
+  }
+}
+
 // Heff = H - (i/2) sum_k L_k^dag L_k ;  M = sum_k l_k l_k^dag
 __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
   const int b = blockIdx.x;
@@ -326,4 +531,62 @@ extern "C" int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream) {
     if (rc != LIME_OK) return rc;
   }
   return LIME_OK;
+}
+
+extern "C" size_t lime_lindblad_adjoint_f64_workspace(int32_t n, int32_t batch, int32_t seg_steps, int32_t k_dense) {
+  if (n <= 0 || batch <= 0 || seg_steps <= 0 || k_dense < 0) return 0;
+  return (size_t)batch * (size_t)f64::adj_ws_mats(seg_steps, k_dense) * (size_t)n * n * sizeof(double2);
+}
+
+template <int TM>
+static int launch_adj(f64::AdjArgs& args, int batch, cudaStream_t st) {
+  const size_t smem = (size_t)(16 * TM) * (f64::kKC + 1) * sizeof(double2) +
+                      (size_t)f64::kKC * (16 * TM + 1) * sizeof(double2);
+  auto kern = f64::lindblad_adjoint_f64_kernel<TM>;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<batch, f64::kThreads, smem, st>>>(args);
+  LIME_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return LIME_OK;
+}
+
+extern "C" int lime_lindblad_adjoint_f64(const LimeAdjointDesc* d, void* stream) {
+  if (!d) return LIME_ERR_ARG;
+  if (d->n <= 0 || d->batch <= 0 || d->seg_steps <= 0 || d->step0 < 0 || d->k_dense < 0 || d->n_obs < 0)
+    return LIME_ERR_ARG;
+  if (d->step0 + d->seg_steps > d->total_steps) return LIME_ERR_ARG;
+  if (!d->ckpt || !d->lam || !d->heff || !d->heff_adj || !d->workspace) return LIME_ERR_ARG;
+  if (!d->grad_diag || !d->grad_bond || !d->grad_gamma) return LIME_ERR_ARG;
+  if (d->k_dense > 0 && (!d->l_dense || !d->l_dense_adj)) return LIME_ERR_ARG;
+  if ((d->m == nullptr) != (d->m_adj == nullptr)) return LIME_ERR_ARG;
+  if (d->n_obs > 0 && (!d->obs_ops || !d->obs_grad)) return LIME_ERR_ARG;
+  if (d->heff_stride < 0 || d->m_stride < 0 || d->l_dense_stride < 0 || d->heff_adj_stride < 0 ||
+      d->m_adj_stride < 0 || d->l_dense_adj_stride < 0 || d->obs_stride < 0)
+    return LIME_ERR_ARG;
+  const int pb = d->param_batch > 0 ? d->param_batch : d->batch;
+  if (pb > d->batch) return LIME_ERR_ARG;
+  if (d->workspace_bytes < lime_lindblad_adjoint_f64_workspace(d->n, d->batch, d->seg_steps, d->k_dense))
+    return LIME_ERR_WORKSPACE;
+  f64::AdjArgs a{};
+  a.n = d->n; a.param_batch = pb; a.seg_steps = d->seg_steps; a.step0 = d->step0;
+  a.total_steps = d->total_steps; a.k_dense = d->k_dense; a.n_obs = d->n_obs; a.obs_diag = d->obs_diag;
+  a.obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  a.obs_per_inst = d->total_steps / a.obs_every;
+  a.dt = d->dt;
+  a.ckpt = reinterpret_cast<const double2*>(d->ckpt);
+  a.lam = reinterpret_cast<double2*>(d->lam);
+  a.heff = reinterpret_cast<const double2*>(d->heff); a.heff_stride = d->heff_stride;
+  a.m = reinterpret_cast<const double2*>(d->m); a.m_stride = d->m_stride;
+  a.ld = reinterpret_cast<const double2*>(d->l_dense); a.ld_stride = d->l_dense_stride;
+  a.heff_adj = reinterpret_cast<const double2*>(d->heff_adj); a.heff_adj_stride = d->heff_adj_stride;
+  a.m_adj = reinterpret_cast<const double2*>(d->m_adj); a.m_adj_stride = d->m_adj_stride;
+  a.ld_adj = reinterpret_cast<const double2*>(d->l_dense_adj); a.ld_adj_stride = d->l_dense_adj_stride;
+  a.obs_ops = reinterpret_cast<const double2*>(d->obs_ops); a.obs_stride = d->obs_stride;
+  a.obs_grad = reinterpret_cast<const double2*>(d->obs_grad);
+  a.g_diag = d->grad_diag; a.g_bond = d->grad_bond; a.g_gamma = d->grad_gamma;
+  a.ws = reinterpret_cast<double2*>(d->workspace);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (d->n <= 16) return launch_adj<1>(a, d->batch, st);
+  if (d->n <= 32) return launch_adj<2>(a, d->batch, st);
+  return launch_adj<4>(a, d->batch, st);
 }

@@ -67,6 +67,7 @@ def _c_layout(struct_name, fields):
     ('LimePrepareDesc', 'PrepareDesc'),
     ('LimeLindbladDesc', 'LindbladDesc'),
     ('LimeLindbladSplitDesc', 'SplitDesc'),
+    ('LimeAdjointDesc', 'AdjointDesc'),
 ])
 def test_descriptor_layout_matches_c(tmp_path, cname, pyname):
     from lime_gb300 import _native
