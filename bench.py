@@ -52,6 +52,7 @@ def parse():
     p.add_argument('--batch', type=int, default=BATCH)
     p.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     p.add_argument('--no-e2e', action='store_true')
+    p.add_argument('--no-adjoint', action='store_true')
     return p.parse_args()
 
 
@@ -218,6 +219,9 @@ def gpu_arm(args, rank, world, local):
     e2e = None
     if not args.no_e2e and rank == 0:
         e2e = e2e_leg(wl, K, path, dev)
+    adj = None
+    if not args.no_adjoint and rank == 0:
+        adj = adjoint_leg(torch, dev)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -264,6 +268,7 @@ def gpu_arm(args, rank, world, local):
         'clocks': clocks,
         'roofline': roof,
         'e2e': e2e,
+        'adjoint': adj,
         'cpu_baseline': cpu,
     }
     if rank == 0:
@@ -294,6 +299,51 @@ def fp64_leg(gen, rho0, pop_ops, K, obs_every, obs_split, torch, engine, k64=4, 
             'split_max_population_error': err,
             'error_sample': 'first %d realisations, all %d steps, every %d-th step recorded'
                             % (n_err, K, max(1, min(obs_every, K)))}
+
+
+def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=0.05):
+    """Adjoint/forward cost on the differentiated absorption workload shape:
+    129-dim chains (|g> + 128 sites), 256 disorder samples, dipole
+    correlation <mu(t) mu(0)>, gradients w.r.t. every site energy, the bond
+    couplings and the dephasing rates, checkpoint every 64 steps.  Times a
+    sample of ``steps`` RK4 steps (the workload runs 4096) of the FP64 path."""
+    import numpy as np
+    from lime_gb300 import chains
+    from lime_gb300.adjoint import chain_observables
+    w = chains.absorption_ensemble(n_sites=n_sites, batch=batch, n_steps=steps, dt=dt)
+    N = n_sites + 1
+    H0 = torch.zeros((N, N), dtype=torch.complex128, device=dev)
+    eps = torch.tensor(w['eps'], device=dev)
+    bond = torch.full((batch, n_sites - 1), w['J'], dtype=torch.float64, device=dev)
+    gamma = torch.full((batch, n_sites), w['gamma'], dtype=torch.float64, device=dev)
+    mu = torch.as_tensor(w['mu'], device=dev)
+    rho0 = mu @ torch.as_tensor(w['rho_g'], device=dev)
+    E = [mu]
+
+    def fwd(req):
+        e = eps.clone().requires_grad_(req)
+        b = bond.clone().requires_grad_(req)
+        g = gamma.clone().requires_grad_(req)
+        return (e, b, g), chain_observables(H0, e, b, g, rho0, E, dt, steps, site0=1,
+                                            checkpoint=checkpoint)
+
+    fwd(False)   # warm
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record()
+    params, obs = fwd(True)
+    ev[1].record()
+    loss = obs.real.sum()   # a linear functional of C(t), as a spectrum is
+    loss.backward()
+    ev[2].record()
+    torch.cuda.synchronize()
+    tf = ev[0].elapsed_time(ev[1]) / 1e3
+    tb = ev[1].elapsed_time(ev[2]) / 1e3
+    return {'workload': 'absorption chain dim %d, %d samples, dipole correlation, grads w.r.t. '
+                        '%d site energies + %d bonds + %d dephasing rates, checkpoint %d'
+                        % (N, batch, n_sites, n_sites - 1, n_sites, checkpoint),
+            'sample_steps': steps, 'path': 'fp64',
+            'forward_s': tf, 'adjoint_s': tb, 'adjoint_over_forward': tb / tf}
 
 
 def e2e_leg(wl, K, path, dev):
