@@ -139,9 +139,9 @@ def measured_peaks():
 def make_workload(batch, rank=0, world=1):
     import numpy as np
     from lime_gb300 import chains
+    from lime_gb300.replicas import shard_range
     w = chains.disorder_ensemble(n=N_SITES, batch=BATCH if batch is None else batch, n_steps=FULL_STEPS)
-    lo = rank * len(w['H']) // world
-    hi = (rank + 1) * len(w['H']) // world
+    lo, hi = shard_range(len(w['H']), rank, world)
     H = w['H'][lo:hi]
     g = w['gamma'][lo:hi]
     # K = n diagonal collapse operators sqrt(gamma_b)|k><k|, given by their diagonals
@@ -202,9 +202,8 @@ def gpu_arm(args, rank, world, local):
     t = ev0.elapsed_time(ev1) / 1e3
     tk = kev[0].elapsed_time(kev[1]) / 1e3
     if world > 1:
-        tt = torch.tensor([t], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t = float(tt.item())
+        from lime_gb300.replicas import max_over_ranks
+        t = max_over_ranks(t, device=dev)
     total_instances = B * world
     value = total_instances * K / t
     clocks = clk.summary()
@@ -240,10 +239,16 @@ def gpu_arm(args, rank, world, local):
                 'peak_source': 'nominal GB300 FP64 (no measured FP64 peak available)'}
     else:
         pk = peaks.get('bf16_tflops_sustained') or 1700.0
-        # issued tensor work: per stage 4 fp16 products of the 128x64x128 real block
-        issued = 4 * 4 * 2 * 128 * 64 * 128
+        # issued tensor work: per stage 5 fp16 products of the 128x64x128 real block
+        issued = 4 * 5 * 2 * 128 * 64 * 128
+        # DRAM traffic per launch: 146.4 KB per instance (ncu capture of 304
+        # instances x 400 steps: 40.5 MB read + 4.0 MB written), scaled by the
+        # instances one full-size launch processes; it does not grow with steps
+        traffic = 146.4e3 * B
         roof = {'bound': 'tensor', 'achieved': achieved_tf, 'peak': pk, 'unit': 'TFLOP/s',
-                'frac': achieved_tf / pk, 'traffic': None,
+                'frac': achieved_tf / pk, 'traffic': traffic,
+                'traffic_source': 'ncu dram__bytes_read+write of a 304-instance launch, '
+                                  'scaled by instances (per-instance, not per-step, traffic)',
                 'peak_source': ('measured bf16 dense sustained (fp16 runs at the same rate), '
                                 'of measured') if peaks else 'fallback 1.7 PFLOP/s',
                 'algorithmic_flop_per_instance_step': flop_per_inst_step,

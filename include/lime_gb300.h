@@ -166,6 +166,55 @@ typedef struct {
 size_t lime_lindblad_adjoint_f64_workspace(int32_t n, int32_t batch, int32_t seg_steps, int32_t k_dense);
 int lime_lindblad_adjoint_f64(const LimeAdjointDesc* d, void* stream);
 
+/* ------------------------------------------------------------------ */
+/* Bloch-Redfield generator and FP64 RK4 on vec(rho)                    */
+/* ------------------------------------------------------------------ */
+
+/* Dense Redfield generator in the eigenbasis of H, row-major Liouville
+ * index a*n+b.  Replaces the N^2 K spectral-density loop and the sparse kron
+ * products of redfield_tensor (lime/oqs.py:528-579); eigh, the eigenbasis
+ * transform A_k = V^dag a_k V and the (user callback) spectra stay with the
+ * caller, as in the reference.
+ *   evals  [n] eigenvalues E
+ *   a_eig  [k][n][n] complex128, A_k in the eigenbasis
+ *   spec   [k|1][n][n] real, C_k[n][m] = S_k(-(E_n - E_m)); spec_stride = 0
+ *          shares one matrix between all k
+ *   R      [n^2][n^2] complex128 out: d vec(rho)/dt = R vec(rho)
+ */
+typedef struct {
+  int32_t n, k;
+  const double* evals;
+  const double* a_eig;
+  const double* spec;     int64_t spec_stride;
+  double* R;
+  void* workspace;        size_t workspace_bytes;
+} LimeRedfieldBuildDesc;
+
+size_t lime_redfield_build_f64_workspace(int32_t n, int32_t k);
+int lime_redfield_build_f64(const LimeRedfieldBuildDesc* d, void* stream);
+
+/* RK4 of a block of right-hand sides vec(rho_r) under a dense generator R in
+ * FP64: replaces the time loop of _redfield (lime/oqs.py:453-462, rhs =
+ * R.dot at 471-472).
+ *   rho     [n^2][n_rhs] complex128 in/out (column r = row-major vec rho_r)
+ *   obs_ops [n_obs][n][n] (eigenbasis); obs_out [n_steps/obs_every][n_rhs][n_obs]
+ *           = Tr(E rho_r) after steps obs_every-1, 2*obs_every-1, ...
+ *   states  [n_steps/states_every][n^2][n_rhs] or NULL
+ */
+typedef struct {
+  int32_t n, n_rhs, n_steps, n_obs, obs_every, states_every;
+  double dt;
+  const double* R;
+  double* rho;
+  const double* obs_ops;
+  double* obs_out;
+  double* states;
+  void* workspace;        size_t workspace_bytes;
+} LimeRedfieldRK4Desc;
+
+size_t lime_redfield_rk4_f64_workspace(int32_t n, int32_t n_rhs);
+int lime_redfield_rk4_f64(const LimeRedfieldRK4Desc* d, void* stream);
+
 /* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate
  * device memory: a host framework whose pool owns the GPU, a latency-critical
  * loop where cudaMalloc/cudaFree would synchronise the device, or a process

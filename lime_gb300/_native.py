@@ -101,6 +101,23 @@ class AdjointDesc(ctypes.Structure):
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
 
 
+class RedfieldBuildDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('k', c_int32),
+                ('evals', c_void_p), ('a_eig', c_void_p),
+                ('spec', c_void_p), ('spec_stride', c_int64),
+                ('R', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
+
+
+class RedfieldRK4Desc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('n_steps', c_int32), ('n_obs', c_int32),
+                ('obs_every', c_int32), ('states_every', c_int32),
+                ('dt', c_double),
+                ('R', c_void_p), ('rho', c_void_p),
+                ('obs_ops', c_void_p), ('obs_out', c_void_p), ('states', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
 SIGNATURES = [
@@ -109,6 +126,10 @@ SIGNATURES = [
     ('lime_lindblad_rk4_f64', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_lindblad_adjoint_f64_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_adjoint_f64', c_int32, [ctypes.POINTER(AdjointDesc), c_void_p]),
+    ('lime_redfield_build_f64_workspace', c_size_t, [c_int32, c_int32]),
+    ('lime_redfield_build_f64', c_int32, [ctypes.POINTER(RedfieldBuildDesc), c_void_p]),
+    ('lime_redfield_rk4_f64_workspace', c_size_t, [c_int32, c_int32]),
+    ('lime_redfield_rk4_f64', c_int32, [ctypes.POINTER(RedfieldRK4Desc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),

@@ -1,0 +1,341 @@
+"""Drop-in for the Bloch-Redfield solvers of ``lime/oqs.py``.
+
+* ``redfield_tensor(H, a_ops, spectra, secular=False)``  lime/oqs.py:528-579
+* ``_redfield(R, rho0, evecs, Nt, dt, t0, e_ops, return_result)``  lime/oqs.py:373-468
+* ``Redfield_solver``  lime/oqs.py:40-371
+
+As in the reference, ``eigh(H)``, the eigenbasis transforms and the user's
+bath spectral callbacks run on the host; the O(N^4 K) assembly of the dense
+generator (``lime_redfield_build_f64``) and the RK4 time loop over a block
+of right-hand sides (``lime_redfield_rk4_f64``) run on the GPU in FP64.  The
+generator is kept on the device in a ``RedfieldTensor``, which offers the
+``toarray()/todense()/shape/dot`` surface of the reference's csr return
+value.  A leading batch axis on ``rho0`` propagates many initial states as
+one GEMM right-hand-side block.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg
+import torch
+
+from . import _native as nat
+from . import engine
+from .result import Result
+
+CDT = torch.complex128
+
+
+def _dense(a):
+    return a.toarray() if hasattr(a, 'toarray') else np.asarray(a)
+
+
+def _isherm(a):
+    return np.allclose(a, a.conj().T)
+
+
+class RedfieldTensor:
+    """Dense Redfield generator (D x D complex128) resident on the GPU."""
+
+    def __init__(self, R: torch.Tensor, n: int):
+        self.R = R
+        self.n = n
+        self.shape = tuple(R.shape)
+
+    def toarray(self):
+        return self.R.cpu().numpy()
+
+    def todense(self):
+        return np.asmatrix(self.toarray())
+
+    def dot(self, x):
+        xt = torch.as_tensor(np.asarray(x), dtype=CDT, device=self.R.device)
+        return (self.R @ xt).cpu().numpy()
+
+    __matmul__ = dot
+
+
+def _spectrum_matrix(S, W):
+    """C[n, m] = S(-W[n, m]): one vectorised call when the callback accepts
+    arrays, else the reference's element-by-element evaluation."""
+    try:
+        C = np.asarray(S(-W), dtype=np.float64)
+        if C.shape == W.shape:
+            return C
+    except Exception:
+        pass
+    n = W.shape[0]
+    C = np.zeros((n, n))
+    for i in range(n):
+        for j in range(n):
+            C[i, j] = S(-W[i, j])
+    return C
+
+
+def redfield_tensor(H, a_ops, spectra, secular=False, device=None):
+    """Bloch-Redfield generator in the eigenbasis of H (lime/oqs.py:528-579).
+
+    Returns ``(R, evecs)`` with d vec(rho)/dt = R vec(rho) (row-major vec);
+    ``secular`` is accepted and ignored, as in the reference.
+    """
+    for a in a_ops:
+        if not _isherm(_dense(a)):
+            raise TypeError("Operators in a_ops must be Hermitian.")
+    lib = nat.require_device()
+    dev = engine._dev(device)
+    Hd = _dense(H)
+    evals, evecs = scipy.linalg.eigh(Hd)
+    n = len(evals)
+    K = len(a_ops)
+    W = np.real(evals[:, None] - evals[None, :])
+    cache = {}
+    Cs = []
+    for k in range(K):
+        key = id(spectra[k])
+        if key not in cache:
+            cache[key] = _spectrum_matrix(spectra[k], W)
+        Cs.append(cache[key])
+    shared = len(cache) == 1
+    A = np.stack([evecs.conj().T @ _dense(a) @ evecs for a in a_ops]).astype(np.complex128)
+    Ct = torch.as_tensor(np.stack([Cs[0]] if shared else Cs), dtype=torch.float64, device=dev).contiguous()
+    At = torch.as_tensor(A, dtype=CDT, device=dev).contiguous()
+    Et = torch.as_tensor(evals, dtype=torch.float64, device=dev).contiguous()
+    D = n * n
+    R = torch.empty((D, D), dtype=CDT, device=dev)
+    wsb = lib.lime_redfield_build_f64_workspace(n, K)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    d = nat.RedfieldBuildDesc()
+    d.n, d.k = n, K
+    d.evals, d.a_eig = Et.data_ptr(), At.data_ptr()
+    d.spec, d.spec_stride = Ct.data_ptr(), (0 if shared else n * n)
+    d.R = R.data_ptr()
+    d.workspace, d.workspace_bytes = ws.data_ptr(), wsb
+    nat.check(lib.lime_redfield_build_f64(d, engine._stream_ptr()), 'lime_redfield_build_f64')
+    return RedfieldTensor(R, n), evecs
+
+
+def _as_generator(R, device):
+    if isinstance(R, RedfieldTensor):
+        return R.R, R.n
+    Rd = torch.as_tensor(_dense(R), dtype=CDT, device=device).contiguous()
+    n = int(round(np.sqrt(Rd.shape[0])))
+    return Rd, n
+
+
+def propagate_vec(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=None, states_every=0,
+                  obs_every=1):
+    """RK4 of eigenbasis density matrices (B, n, n) under the dense generator.
+
+    Returns (obs (B, n_steps // obs_every, n_obs), states (B, S, n, n) or None,
+    final rho (B, n, n)), all in the eigenbasis.
+    """
+    lib = nat.require_device()
+    Rd, n = R
+    dev = Rd.device
+    B = rho0_eb.shape[0]
+    D = n * n
+    P = rho0_eb.reshape(B, D).transpose(0, 1).contiguous()          # D x B, column = vec rho
+    E = None
+    n_obs = 0
+    if e_eb is not None and len(e_eb):
+        E = torch.stack(list(e_eb)).to(CDT).contiguous()
+        n_obs = E.shape[0]
+    n_slots = n_steps // obs_every
+    obs = torch.zeros((max(n_slots, 1), B, max(n_obs, 1)), dtype=CDT, device=dev)
+    states = None
+    if states_every:
+        states = torch.empty((n_steps // states_every, D, B), dtype=CDT, device=dev)
+    wsb = lib.lime_redfield_rk4_f64_workspace(n, B)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    d = nat.RedfieldRK4Desc()
+    d.n, d.n_rhs, d.n_steps, d.n_obs = n, B, n_steps, n_obs
+    d.obs_every, d.states_every = obs_every, states_every if states is not None else 0
+    d.dt = float(dt)
+    d.R, d.rho = Rd.data_ptr(), P.data_ptr()
+    if E is not None:
+        d.obs_ops, d.obs_out = E.data_ptr(), obs.data_ptr()
+    d.states = None if states is None else states.data_ptr()
+    d.workspace, d.workspace_bytes = ws.data_ptr(), wsb
+    nat.check(lib.lime_redfield_rk4_f64(d, engine._stream_ptr()), 'lime_redfield_rk4_f64')
+    o = obs[:n_slots, :, :n_obs].permute(1, 0, 2)
+    st = None
+    if states is not None:
+        st = states.permute(2, 0, 1).reshape(B, -1, n, n)
+    return o, st, P.transpose(0, 1).reshape(B, n, n)
+
+
+def _redfield(R, rho0, evecs=None, Nt=1, dt=0.005, t0=0, e_ops=None, return_result=True,
+              store_states=True):
+    """RK4 of the Redfield equation (lime/oqs.py:373-468).
+
+    ``return_result=True``: a ``Result`` with ``observables`` (Nt, n_e)
+    evaluated in the eigenbasis at t = (k+1) dt and ``rholist`` transformed
+    back to the site basis.  ``return_result=False``: writes ``obs.dat``
+    (observables before each step) and returns the final vec(rho).
+    A batch of initial states (B, n, n) gives (B, Nt, n_e) observables.
+    """
+    e_ops = [] if e_ops is None else list(e_ops)
+    dev = engine._dev(None)
+    Rg = _as_generator(R, dev)
+    n = Rg[1]
+    r0 = np.asarray(_dense(rho0) if np.ndim(rho0) == 2 else rho0)
+    batched = r0.ndim == 3
+    r0 = r0.reshape((-1, n, n)).astype(np.complex128)
+    V = None if evecs is None else torch.as_tensor(np.asarray(evecs), dtype=CDT, device=dev)
+    r0t = torch.as_tensor(r0, dtype=CDT, device=dev)
+    if V is not None:
+        r0t = V.mH @ r0t @ V
+    e_eb = [torch.as_tensor(_dense(e), dtype=CDT, device=dev) for e in e_ops]
+    if V is not None:
+        e_eb = [V.mH @ e @ V for e in e_eb]
+    if not return_result:
+        o, _, rho = propagate_vec(Rg, r0t, dt, Nt, e_eb)
+        first = torch.stack([torch.einsum('ji,bij->b', e, r0t) for e in e_eb], -1) if e_eb else None
+        ob = o[0].cpu().numpy()
+        rows = [first[0].cpu().numpy()] + [ob[k] for k in range(Nt - 1)] if e_eb else [[]] * Nt
+        fmt = '{} ' * (len(e_ops) + 1) + '\n'
+        with open('obs.dat', 'w') as f:
+            t = t0
+            for k in range(Nt):
+                t += dt
+                f.write(fmt.format(t, *rows[k]))
+        out = rho.reshape(rho.shape[0], -1).cpu().numpy()
+        return out if batched else out[0]
+    o, st, rho = propagate_vec(Rg, r0t, dt, Nt, e_eb, states_every=1 if store_states else 0)
+    res = Result(dt=dt, Nt=Nt, rho0=rho0, t0=t0, nout=1)
+    obs_np = o.cpu().numpy()
+    res.observables = obs_np if batched else obs_np[0]
+    if st is not None:
+        if V is not None:
+            st = V @ st @ V.mH
+        stn = st.cpu().numpy()
+        res.rholist = stn if batched else list(stn[0])
+    else:
+        fin = rho if V is None else V @ rho @ V.mH
+        res.rholist = fin.cpu().numpy() if batched else [fin[0].cpu().numpy()]
+    return res
+
+
+class Redfield_solver:
+    """Bloch-Redfield solver (lime/oqs.py:40-371)."""
+
+    def __init__(self, H, c_ops=None, spectra=None, e_ops=None):
+        self.H = H
+        self.c_ops = c_ops
+        self.R = None
+        self.spectra = spectra
+        self.evecs = None
+        self.dim = H.shape[0]
+        self.U = None
+        self.G = None
+        self.e_ops = e_ops
+
+    def idm(self, sp=True):
+        from scipy.sparse import identity
+        from .superoperator import dm2vec
+        return dm2vec(identity(self.dim)) if sp else dm2vec(identity(self.dim).toarray())
+
+    def configure(self, H, c_ops, e_ops):
+        self.c_ops = c_ops
+        self.e_ops = e_ops
+        self.H = H
+
+    def redfield_tensor(self, secular=False):
+        if self.spectra is None:
+            raise TypeError('Specify the bath spectral function.')
+        R, evecs = redfield_tensor(self.H, self.c_ops, self.spectra, secular)
+        self.R = R
+        self.evecs = evecs
+        return R, evecs
+
+    def evolve(self, rho0, dt, Nt, evecs=None, e_ops=[], store_states=False, t0=0, nout=1):
+        if self.R is None:
+            self.redfield_tensor()
+        return _redfield(self.R, rho0, evecs=self.evecs, Nt=Nt, dt=dt, t0=t0, e_ops=e_ops)
+
+    def steady_state(self):
+        pass
+
+    # ---------------- Green's-function route (lime/oqs.py:169-366)
+    def propagator(self, t, method='SOS'):
+        """U(t) = exp(R t) for the times t, shape (D, D, len(t)).
+
+        ``method='SOS'``: eigen-decomposition of R (lime/oqs.py:205-216);
+        ``'EOM'``: RK4 of U with the generator (lime/oqs.py:195-203, the
+        reference's expm(A, t) integrates dU/dt = A U on the grid t).
+        """
+        if self.R is None:
+            raise TypeError('Redfield tensor is not computed. Please call redfield_tensor()')
+        t = np.asarray(t, dtype=np.float64)
+        Rd = self.R.R
+        if method in ('eseries', 'SOS'):
+            w, U1 = torch.linalg.eig(Rd)
+            U2 = torch.linalg.inv(U1)
+            tt = torch.as_tensor(t, dtype=torch.float64, device=Rd.device)
+            Et = torch.exp(w[:, None] * tt[None, :])
+            U = torch.einsum('aj,jk,jb->abk', U1, Et, U2)
+        elif method == 'EOM':
+            n = self.R.n
+            D = n * n
+            eye = torch.eye(D, dtype=CDT, device=Rd.device).reshape(D, n, n)
+            dt = t[1] - t[0] if len(t) > 1 else 0.0
+            Us = [torch.eye(D, dtype=CDT, device=Rd.device)]
+            if len(t) > 1:
+                _, st, _ = propagate_vec((Rd, n), eye, dt, len(t) - 1, None, states_every=1)
+                for k in range(len(t) - 1):
+                    Us.append(st[:, k].reshape(D, D).transpose(0, 1))
+            U = torch.stack(Us, -1)
+        else:
+            raise NotImplementedError('Method of {} has not been implemented.'.format(method))
+        self.U = U
+        self.G = -1j * U
+        return U.cpu().numpy()
+
+    def expect(self, rho0, e_ops):
+        V = np.asarray(self.evecs)
+        rho0_eb = (V.conj().T @ _dense(rho0) @ V).flatten()
+        U = self.U
+        rho = torch.tensordot(U, torch.as_tensor(rho0_eb, dtype=CDT, device=U.device), dims=([1], [0]))
+        out = np.zeros((U.shape[-1], len(e_ops)), dtype=np.complex128)
+        for j, e in enumerate(e_ops):
+            ev = torch.as_tensor((V.conj().T @ _dense(e) @ V).flatten(), dtype=CDT, device=U.device)
+            out[:, j] = (ev @ rho).cpu().numpy()
+        return out
+
+    def correlation_2op_1t(self, rho0, a, b, tau):
+        """<<I| a G(tau) b |rho0>> (lime/oqs.py:254-275) with a dense identity
+        vector (the reference's sparse one cannot be contracted)."""
+        if self.G is None:
+            self.propagator(tau)
+        G = self.G
+        dev = G.device
+        idm = torch.as_tensor(np.identity(self.dim).flatten(), dtype=CDT, device=dev)
+        r = _dense(rho0)
+        if r.ndim == 2:
+            r = r.flatten()
+        at = torch.as_tensor(_dense(a), dtype=CDT, device=dev)
+        bt = torch.as_tensor(_dense(b), dtype=CDT, device=dev)
+        x = bt @ torch.as_tensor(r, dtype=CDT, device=dev)
+        y = torch.tensordot(G, x, dims=([1], [0]))
+        return (idm @ (at @ y)).cpu().numpy()
+
+    def correlation_4op_3t(self, rho0, oplist, signature, tau):
+        """<<I|A G(t3) B G(t2) C G(t1) D|rho0>> (lime/oqs.py:277-366)."""
+        from .superoperator import operator_to_superoperator
+        if len(oplist) != 4:
+            raise ValueError('Number of operators is not 4.')
+        if self.G is None:
+            self.propagator(tau)
+        G = self.G
+        dev = G.device
+        ops = [torch.as_tensor(operator_to_superoperator(o, s).toarray(), dtype=CDT, device=dev)
+               for o, s in zip(oplist, signature)]
+        a, b, c, d = ops
+        idm = torch.as_tensor(np.identity(self.dim).flatten(), dtype=CDT, device=dev)
+        rho = d @ torch.as_tensor(_dense(rho0).flatten(), dtype=CDT, device=dev)
+        tmp = torch.tensordot(G, rho, dims=([1], [0]))
+        tmp = c @ tmp
+        tmp = torch.tensordot(G, tmp, dims=([1], [0]))
+        tmp = torch.tensordot(b, tmp, dims=([1], [0]))
+        tmp = torch.tensordot(G, tmp, dims=([1], [0]))
+        return torch.einsum('a,ab,bijk->ijk', idm, a, tmp).cpu().numpy()

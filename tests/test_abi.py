@@ -68,6 +68,8 @@ def _c_layout(struct_name, fields):
     ('LimeLindbladDesc', 'LindbladDesc'),
     ('LimeLindbladSplitDesc', 'SplitDesc'),
     ('LimeAdjointDesc', 'AdjointDesc'),
+    ('LimeRedfieldBuildDesc', 'RedfieldBuildDesc'),
+    ('LimeRedfieldRK4Desc', 'RedfieldRK4Desc'),
 ])
 def test_descriptor_layout_matches_c(tmp_path, cname, pyname):
     from lime_gb300 import _native
