@@ -117,6 +117,13 @@ typedef struct {
   double* states;
   void* workspace;        size_t workspace_bytes;
   int32_t* status;
+  /* time-dependent Hamiltonian H(t) = H0 - sum_q f_q(t) H_q (the driven
+   * solver, lime/oqs.py:1691-1800): drive_ops [n_drive][n][n] complex128
+   * Hermitian, drive_coef [n_steps][n_drive] real f_q(t0 + (k+1) dt) for
+   * step k of this call.  n_drive = 0 for a static generator. */
+  int32_t n_drive;
+  const double* drive_ops;
+  const double* drive_coef;
 } LimeLindbladDesc;
 
 size_t lime_lindblad_rk4_f64_workspace(int32_t n, int32_t batch, int32_t k_dense);

@@ -21,8 +21,8 @@ namespace f64 {
 constexpr int kThreads = 256;
 constexpr int kKC = 16;  // k-chunk of the shared-memory tiles
 
-// Workspace layout per instance (complex elements): rs | X | acc | [Y | J]
-__host__ __device__ inline int64_t ws_mats(int k_dense) { return k_dense > 0 ? 5 : 3; }
+// Workspace layout per instance (complex elements): rs | X | acc | [Y | J] | Heff(t)
+__host__ __device__ inline int64_t ws_mats(int k_dense) { return k_dense > 0 ? 6 : 4; }
 
 // C (+)= A * op(B), all n x n, row-major, global memory; whole CTA.
 // op(B) = B (conjb = false) or B^dag (conjb = true).
@@ -105,6 +105,9 @@ struct RK4Args {
   double2* ws;
   double* tr0;
   int32_t* status;
+  int n_drive;
+  const double2* drive_ops;
+  const double* drive_coef;
 };
 
 template <int TM>
@@ -116,7 +119,7 @@ __global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
   const int64_t nn = (int64_t)n * n;
   const int p = b % a.param_batch;
   double2* rho = a.rho + b * nn;
-  const double2* heff = a.heff + p * a.heff_stride;
+  const double2* heff0 = a.heff + p * a.heff_stride;
   const double2* m = a.m ? a.m + p * a.m_stride : nullptr;
   const double2* ld = a.l_dense ? a.l_dense + p * a.l_dense_stride : nullptr;
   const double2* obs_ops = a.obs_ops ? a.obs_ops + p * a.obs_stride : nullptr;
@@ -126,6 +129,7 @@ __global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
   double2* acc = ws + 2 * nn;
   double2* Y = ws + 3 * nn;
   double2* J = ws + 4 * nn;
+  double2* heff_t = ws + (ws_mats(a.k_dense) - 1) * nn;
 
   // trace at the start of the call (first chunk) for the drift check
   if (a.step0 == 0) {
@@ -141,6 +145,19 @@ __global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
   const double dt = a.dt, dt2 = a.dt / 2.0;
   int flags = 0;
   for (int step = 0; step < a.n_steps; ++step) {
+    // driven generator (lime/oqs.py:1716-1722): Heff(t) = Heff0 - sum_i f_i(t) H_i
+    // with f_i evaluated at the end of the step
+    const double2* heff = heff0;
+    if (a.n_drive > 0) {
+      const double* c = a.drive_coef + (int64_t)(a.step0 + step) * a.n_drive;
+      for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
+        double2 v = heff0[e];
+        for (int q = 0; q < a.n_drive; ++q) v = csub(v, cscale(a.drive_ops[q * nn + e], c[q]));
+        heff_t[e] = v;
+      }
+      __syncthreads();
+      heff = heff_t;
+    }
 #pragma unroll 1
     for (int s = 0; s < 4; ++s) {
       cta_cgemm<TM>(heff, rs, false, X, false, n, smem);
@@ -495,6 +512,7 @@ extern "C" int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream) {
   const int pb = d->param_batch > 0 ? d->param_batch : d->batch;
   if (pb > d->batch) return LIME_ERR_ARG;
   if (!(d->dt == d->dt)) return LIME_ERR_ARG;
+  if (d->n_drive < 0 || (d->n_drive > 0 && (!d->drive_ops || !d->drive_coef))) return LIME_ERR_ARG;
   if (d->workspace_bytes < lime_lindblad_rk4_f64_workspace(d->n, d->batch, d->k_dense))
     return LIME_ERR_WORKSPACE;
   if (d->n_steps == 0) return LIME_OK;
@@ -518,6 +536,9 @@ extern "C" int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream) {
   a.tr0 = reinterpret_cast<double*>(reinterpret_cast<char*>(d->workspace) +
                                     (size_t)d->batch * f64::ws_mats(d->k_dense) * nn * sizeof(double2));
   a.status = d->status;
+  a.n_drive = d->n_drive;
+  a.drive_ops = reinterpret_cast<const double2*>(d->drive_ops);
+  a.drive_coef = d->drive_coef;
   // bounded launches: at most ~2^27 complex MACs of GEMM per instance per launch
   const double per_step = 4.0 * (1 + 2 * d->k_dense) * (double)nn * d->n;
   int chunk = (int)fmax(1.0, fmin((double)d->n_steps, 134217728.0 / per_step));

@@ -183,7 +183,7 @@ def prepare_obs(e_ops, n, P, device):
 
 def _run_f64(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int,
              obs, obs_every: int, states_every: int, trace_tol: float, param_batch: int,
-             events=None):
+             events=None, drive=None):
     lib = nat.require_device()
     B, n = rho.shape[0], gen.n
     Et, n_obs, obs_diag, obs_stride = obs
@@ -212,6 +212,9 @@ def _run_f64(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int,
     d.states = _ptr(states)
     d.workspace, d.workspace_bytes = ws.data_ptr(), wsb
     d.status = status.data_ptr()
+    if drive is not None:
+        ops, coef = drive
+        d.n_drive, d.drive_ops, d.drive_coef = ops.shape[0], ops.data_ptr(), coef.data_ptr()
     if events is not None:
         events[0].record()
     nat.check(lib.lime_lindblad_rk4_f64(d, _stream_ptr()), 'lime_lindblad_rk4_f64')
@@ -300,7 +303,7 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
 
 def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
               states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
-              check: bool = True, obs_every: int = 1, events=None):
+              check: bool = True, obs_every: int = 1, events=None, drive=None):
     """RK4-propagate density matrices under ``gen``.
 
     ``rho0``: (n, n) or (B, n, n); with a non-shared generator B must equal
@@ -309,6 +312,8 @@ def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     obs_every-1, 2 obs_every-1, ..., ``states`` (B, n_steps // states_every,
     n, n) or None, ``rho`` (B, n, n) final.  ``events``: optional pair of
     CUDA events recorded on the launching stream around the kernel call.
+    ``drive``: optional (ops (q, n, n), coef (n_steps, q) float64) device
+    tensors for H(t) = H0 - sum_q coef[k, q] ops[q] during step k (FP64 path).
     """
     if obs_every < 1 or states_every < 0 or n_steps < 0:
         raise ValueError('obs_every must be >= 1, states_every >= 0, n_steps >= 0')
@@ -336,8 +341,11 @@ def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     if precision == 'fp64':
         tol = 1e-9 if trace_tol is None else trace_tol
         o, s, status = _run_f64(gen, work, dt, n_steps, obs, obs_every, states_every, tol,
-                                param_batch=B, events=events)
+                                param_batch=B, events=events, drive=drive)
     elif precision == 'split':
+        if drive is not None:
+            raise ValueError('precision="split" propagates static generators; use "fp64" for '
+                             'time-dependent Hamiltonians')
         if states_every:
             raise ValueError('precision="split" keeps the state on chip; states_every is not '
                              'supported (use precision="fp64" for rholist output)')

@@ -42,10 +42,10 @@ def test_status_strings(lib):
 
 
 def test_workspace_query(lib):
-    # 3 matrices per instance (+ one trace double), 5 with dense collapse ops
+    # 4 matrices per instance (+ one trace double), 6 with dense collapse ops
     n, b = 16, 3
-    assert lib.lime_lindblad_rk4_f64_workspace(n, b, 0) == b * (3 * n * n * 16 + 8)
-    assert lib.lime_lindblad_rk4_f64_workspace(n, b, 2) == b * (5 * n * n * 16 + 8)
+    assert lib.lime_lindblad_rk4_f64_workspace(n, b, 0) == b * (4 * n * n * 16 + 8)
+    assert lib.lime_lindblad_rk4_f64_workspace(n, b, 2) == b * (6 * n * n * 16 + 8)
     assert lib.lime_lindblad_rk4_f64_workspace(0, b, 0) == 0
 
 

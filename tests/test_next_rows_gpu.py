@@ -1,0 +1,106 @@
+"""Driven Lindblad, spectra and the eigen-series solver vs the reference's golden vectors."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import load_golden
+from lime_gb300 import chains
+
+RTOL = 1e-10
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+
+
+def test_fft_convention_cpu():
+    from lime_gb300.spectra import fft
+    g = load_golden('fft')
+    gg, freq = fft(g['f'], g['x'], device='cpu')
+    assert rel(gg, g['g']) < 1e-13 and rel(freq, g['freq']) < 1e-15
+
+
+@pytest.fixture(scope='module')
+def lib():
+    from lime_gb300 import build, _native
+    build.build()
+    return _native.require_device()
+
+
+@pytest.mark.gpu
+def test_driven_matches_reference(lib):
+    from lime_gb300.oqs import Lindblad_solver
+    g = load_golden('driven_n4')
+    f = lambda t: 0.1 * np.sin(t)
+    sol = Lindblad_solver([g['H0'], [g['H1'], f]], c_ops=list(g['c_ops']))
+    res = sol.evolve(chains.ground_dm(4), dt=float(g['dt']), Nt=int(g['Nt']),
+                     e_ops=chains.population_ops(4))
+    assert rel(res.observables, g['observables']) < RTOL
+    assert rel(res.rholist[-1], g['rho_final']) < RTOL
+
+
+@pytest.mark.gpu
+def test_driven_complex_coefficients_rejected(lib):
+    from lime_gb300.driven import _lindblad_driven
+    H0 = np.eye(2, dtype=complex)
+    with pytest.raises(ValueError):
+        _lindblad_driven([H0, [np.eye(2), lambda t: 1j * t]], chains.ground_dm(2), Nt=2, dt=0.1)
+
+
+@pytest.mark.gpu
+def test_fft_on_device_matches_reference(lib):
+    from lime_gb300.spectra import fft
+    g = load_golden('fft')
+    gg, freq = fft(torch.as_tensor(g['f'], device='cuda'), g['x'])
+    assert rel(gg.cpu().numpy(), g['g']) < 1e-13
+
+
+def test_eigen_series_solver_matches_reference():
+    from lime_gb300.superoperator import Lindblad_solver
+    g = load_golden('superop_n4')
+    es = Lindblad_solver(g['H'], c_ops=list(g['c_ops']))
+    es.eigenstates()
+    ev = es.evolve(chains.ground_dm(4), g['t'], list(g['e_ops'])).observables
+    assert rel(ev, g['evolve']) < 1e-9
+    cc = es.correlation_2op_1t(chains.ground_dm(4), [g['a'], g['a']], g['t'])
+    assert rel(cc, g['cor']) < 1e-9
+
+
+@pytest.mark.gpu
+def test_eigen_series_two_time_vs_rk4(lib):
+    """The eigen-series 3op_2t agrees with the RK4 drop-in up to RK4 truncation."""
+    from lime_gb300.superoperator import Lindblad_solver as ES
+    from lime_gb300.oqs import Lindblad_solver
+    rng = np.random.default_rng(4)
+    H, c_ops = chains.uneven_chain(4, rng, n_ops=2)
+    ops = [rng.normal(size=(4, 4)) + 1j * rng.normal(size=(4, 4)) for _ in range(3)]
+    dt, Nt, Ntau = 0.02, 6, 5
+    rk = Lindblad_solver(H, c_ops=c_ops).correlation_3op_2t(chains.ground_dm(4), ops, dt, Nt, Ntau)
+    es = ES(H, c_ops, exact_norm=True)
+    es.eigenstates()
+    t = dt * np.arange(1, Nt + 1)
+    tau = dt * np.arange(1, Ntau + 1)
+    ex = es.correlation_3op_2t(chains.ground_dm(4), ops, t, tau).T
+    assert rel(rk, ex) < 1e-7
+
+
+@pytest.mark.gpu
+def test_spectrum_gradient_flows_through_adjoint(lib):
+    from lime_gb300.adjoint import chain_observables
+    from lime_gb300.spectra import correlation_spectrum
+    dev = torch.device('cuda')
+    ns, N = 4, 5
+    eps = torch.zeros((1, ns), dtype=torch.float64, device=dev, requires_grad=True)
+    bond = torch.full((1, ns - 1), -0.1, dtype=torch.float64, device=dev, requires_grad=True)
+    gamma = torch.full((1, ns), 0.02, dtype=torch.float64, device=dev, requires_grad=True)
+    mu = torch.zeros((N, N), dtype=torch.complex128, device=dev)
+    mu[0, 1:] = 1.0
+    mu[1:, 0] = 1.0
+    rho0 = mu @ torch.as_tensor(chains.ground_dm(N), device=dev)
+    H0 = torch.zeros((N, N), dtype=torch.complex128, device=dev)
+    cor = chain_observables(H0, eps, bond, gamma, rho0, [mu], 0.05, 64, site0=1, checkpoint=16)
+    spec, w = correlation_spectrum(cor[0, :, 0], 0.05)
+    spec.real.max().backward()
+    assert torch.isfinite(eps.grad).all() and eps.grad.abs().sum() > 0
+    assert torch.isfinite(gamma.grad).all() and gamma.grad.abs().sum() > 0
