@@ -54,6 +54,8 @@ typedef enum {
 #define LIME_FLAG_NONFINITE   0x1  /* a NaN/Inf appeared in rho            */
 #define LIME_FLAG_TRACE_DRIFT 0x2  /* |Tr rho(t) - Tr rho(0)| > trace_tol   */
 #define LIME_FLAG_TIMEOUT     0x4  /* a bounded device-side wait expired    */
+#define LIME_FLAG_RANGE       0x8  /* a split-precision operand left its    */
+                                   /* fixed-point range (rescale and rerun) */
 
 /* ------------------------------------------------------------------ */
 /* Generator preparation                                               */
@@ -221,6 +223,35 @@ typedef struct {
 
 size_t lime_redfield_rk4_f64_workspace(int32_t n, int32_t n_rhs);
 int lime_redfield_rk4_f64(const LimeRedfieldRK4Desc* d, void* stream);
+
+/* The same RK4 on the tcgen05 tensor cores in split precision: per stage
+ * one GEMM [Yr|Yi] = [Lr|Li] . [[Sr,Si],[-Si,Sr]] with the operands streamed
+ * by bulk copies from pre-tiled fp16 pieces (A = R: per-row 7-bit fixed
+ * point + two fp16 residuals; B = stage input: 10-bit fixed point + fp16
+ * residual), exact dominant product, fp32 two-sum accumulation, RK4 state
+ * in fp32 hi + lo.  Replaces the same loop as lime_redfield_rk4_f64.
+ *   R        [n^2][n^2] complex128 (from lime_redfield_build_f64)
+ *   rho      [n_rhs][n^2] complex128 in/out, row-major vec(rho_r) per RHS
+ *   scale_a_log2  R * 2^a with max |R| ~ 2^12
+ *   scale_b_log2  rho * 2^b with max |rho| * 1.25 <= 2^13
+ *   obs_ops  [n_obs][n][n]; obs_out [n_steps/obs_every][n_rhs][n_obs]
+ *   workspace lime_redfield_split_workspace() bytes, 1024-byte aligned
+ *   status   device int32 (LIME_FLAG_* bits)
+ */
+typedef struct {
+  int32_t n, n_rhs, n_steps, n_obs, obs_every;
+  int32_t scale_a_log2, scale_b_log2;
+  double dt;
+  const double* R;
+  double* rho;
+  const double* obs_ops;
+  double* obs_out;
+  void* workspace;        size_t workspace_bytes;
+  int32_t* status;
+} LimeRedfieldSplitDesc;
+
+size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs);
+int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* stream);
 
 /* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate
  * device memory: a host framework whose pool owns the GPU, a latency-critical

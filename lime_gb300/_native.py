@@ -21,6 +21,7 @@ c_size_t = ctypes.c_size_t
 LIME_FLAG_NONFINITE = 0x1
 LIME_FLAG_TRACE_DRIFT = 0x2
 LIME_FLAG_TIMEOUT = 0x4
+LIME_FLAG_RANGE = 0x8
 
 
 class LimeError(RuntimeError):
@@ -43,6 +44,8 @@ class KernelFlagError(RuntimeError):
             names.append('trace drift above tolerance')
         if flags & LIME_FLAG_TIMEOUT:
             names.append('device-side wait timed out')
+        if flags & LIME_FLAG_RANGE:
+            names.append('split-precision operand outside its fixed-point range')
         super().__init__('%s: %s (flags 0x%x)' % (where, ', '.join(names) or 'unknown', flags))
 
 
@@ -119,6 +122,16 @@ class RedfieldRK4Desc(ctypes.Structure):
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
 
 
+class RedfieldSplitDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('n_steps', c_int32), ('n_obs', c_int32),
+                ('obs_every', c_int32), ('scale_a_log2', c_int32), ('scale_b_log2', c_int32),
+                ('dt', c_double),
+                ('R', c_void_p), ('rho', c_void_p),
+                ('obs_ops', c_void_p), ('obs_out', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t),
+                ('status', c_void_p)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
 SIGNATURES = [
@@ -131,6 +144,8 @@ SIGNATURES = [
     ('lime_redfield_build_f64', c_int32, [ctypes.POINTER(RedfieldBuildDesc), c_void_p]),
     ('lime_redfield_rk4_f64_workspace', c_size_t, [c_int32, c_int32]),
     ('lime_redfield_rk4_f64', c_int32, [ctypes.POINTER(RedfieldRK4Desc), c_void_p]),
+    ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32]),
+    ('lime_redfield_rk4_split', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),

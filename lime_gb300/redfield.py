@@ -164,8 +164,94 @@ def propagate_vec(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=None, 
     return o, st, P.transpose(0, 1).reshape(B, n, n)
 
 
+def _pow2_floor(x: float) -> int:
+    return int(np.floor(np.log2(x)))
+
+
+def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=None, obs_every=1,
+                        max_retries=3):
+    """Tensor-core split-precision RK4 (``lime_redfield_rk4_split``) of
+    eigenbasis density matrices (B, n, n) under the dense generator.
+
+    Same returns as ``propagate_vec`` without states.  The generator is
+    scaled to max |R| ~ 2^12 and the states to max |rho0| * 1.25 <= 2^13
+    (powers of two, so the scaling is exact); a run whose states leave the
+    fixed-point range raises LIME_FLAG_RANGE and is repeated with the state
+    scale lowered by 4x.
+    """
+    lib = nat.require_device()
+    Rd, n = R
+    dev = Rd.device
+    B = rho0_eb.shape[0]
+    D = n * n
+    E = None
+    n_obs = 0
+    if e_eb is not None and len(e_eb):
+        E = torch.stack(list(e_eb)).to(CDT).contiguous()
+        n_obs = E.shape[0]
+    n_slots = n_steps // obs_every
+    rmax = float(torch.view_as_real(Rd).abs().max().item()) if Rd.numel() else 0.0
+    pmax = float(torch.view_as_real(rho0_eb).abs().max().item()) if rho0_eb.numel() else 0.0
+    sa = _pow2_floor(4096.0 / rmax) if rmax > 0 else 0
+    sb = _pow2_floor(8192.0 / (1.25 * pmax)) if pmax > 0 else 0
+    sa = max(-60, min(60, sa))
+    wsb = lib.lime_redfield_split_workspace(n, B)
+    ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
+    base = ws.data_ptr()
+    aligned = (base + 1023) // 1024 * 1024
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    for attempt in range(max_retries + 1):
+        P = rho0_eb.reshape(B, D).to(CDT).contiguous().clone()        # [R][D], row = vec rho
+        obs = torch.zeros((max(n_slots, 1), B, max(n_obs, 1)), dtype=CDT, device=dev)
+        status.zero_()
+        d = nat.RedfieldSplitDesc()
+        d.n, d.n_rhs, d.n_steps, d.n_obs, d.obs_every = n, B, n_steps, n_obs, obs_every
+        d.scale_a_log2, d.scale_b_log2 = sa, max(-60, min(60, sb))
+        d.dt = float(dt)
+        d.R, d.rho = Rd.data_ptr(), P.data_ptr()
+        if E is not None:
+            d.obs_ops, d.obs_out = E.data_ptr(), obs.data_ptr()
+        d.workspace, d.workspace_bytes = aligned, wsb
+        d.status = status.data_ptr()
+        nat.check(lib.lime_redfield_rk4_split(d, engine._stream_ptr()), 'lime_redfield_rk4_split')
+        flags = int(status.item())
+        if flags & nat.LIME_FLAG_RANGE and attempt < max_retries:
+            sb -= 2
+            continue
+        if flags:
+            raise nat.KernelFlagError(flags, 'lime_redfield_rk4_split')
+        break
+    o = obs[:n_slots, :, :n_obs].permute(1, 0, 2)
+    return o, None, P.reshape(B, n, n)
+
+
+def _propagate(Rg, r0t, dt, Nt, e_eb, states_every=0, precision='fp64'):
+    if precision == 'fp64':
+        return propagate_vec(Rg, r0t, dt, Nt, e_eb, states_every=states_every)
+    if precision != 'split':
+        raise ValueError("precision must be 'fp64' or 'split'")
+    if not states_every:
+        return propagate_vec_split(Rg, r0t, dt, Nt, e_eb)
+    # states every `states_every` steps: segments of split runs restarted
+    # from each segment's complex128 end state
+    n = Rg[1]
+    obs_parts, states = [], []
+    rho = r0t
+    done = 0
+    while done < Nt:
+        m = min(states_every, Nt - done)
+        o, _, rho = propagate_vec_split(Rg, rho, dt, m, e_eb)
+        obs_parts.append(o)
+        if m == states_every:
+            states.append(rho)
+        done += m
+    o = torch.cat(obs_parts, 1)
+    st = torch.stack(states, 1) if states else None
+    return o, st, rho
+
+
 def _redfield(R, rho0, evecs=None, Nt=1, dt=0.005, t0=0, e_ops=None, return_result=True,
-              store_states=True):
+              store_states=True, precision='fp64'):
     """RK4 of the Redfield equation (lime/oqs.py:373-468).
 
     ``return_result=True``: a ``Result`` with ``observables`` (Nt, n_e)
@@ -173,6 +259,9 @@ def _redfield(R, rho0, evecs=None, Nt=1, dt=0.005, t0=0, e_ops=None, return_resu
     back to the site basis.  ``return_result=False``: writes ``obs.dat``
     (observables before each step) and returns the final vec(rho).
     A batch of initial states (B, n, n) gives (B, Nt, n_e) observables.
+    ``precision='split'`` runs the RK4 on the tensor cores
+    (``propagate_vec_split``); stored states then come from restarting the
+    split run every step, so pass ``store_states=False`` for long runs.
     """
     e_ops = [] if e_ops is None else list(e_ops)
     dev = engine._dev(None)
@@ -189,7 +278,7 @@ def _redfield(R, rho0, evecs=None, Nt=1, dt=0.005, t0=0, e_ops=None, return_resu
     if V is not None:
         e_eb = [V.mH @ e @ V for e in e_eb]
     if not return_result:
-        o, _, rho = propagate_vec(Rg, r0t, dt, Nt, e_eb)
+        o, _, rho = _propagate(Rg, r0t, dt, Nt, e_eb, precision=precision)
         first = torch.stack([torch.einsum('ji,bij->b', e, r0t) for e in e_eb], -1) if e_eb else None
         ob = o[0].cpu().numpy()
         rows = [first[0].cpu().numpy()] + [ob[k] for k in range(Nt - 1)] if e_eb else [[]] * Nt
@@ -201,7 +290,8 @@ def _redfield(R, rho0, evecs=None, Nt=1, dt=0.005, t0=0, e_ops=None, return_resu
                 f.write(fmt.format(t, *rows[k]))
         out = rho.reshape(rho.shape[0], -1).cpu().numpy()
         return out if batched else out[0]
-    o, st, rho = propagate_vec(Rg, r0t, dt, Nt, e_eb, states_every=1 if store_states else 0)
+    o, st, rho = _propagate(Rg, r0t, dt, Nt, e_eb, states_every=1 if store_states else 0,
+                            precision=precision)
     res = Result(dt=dt, Nt=Nt, rho0=rho0, t0=t0, nout=1)
     obs_np = o.cpu().numpy()
     res.observables = obs_np if batched else obs_np[0]
@@ -248,10 +338,13 @@ class Redfield_solver:
         self.evecs = evecs
         return R, evecs
 
-    def evolve(self, rho0, dt, Nt, evecs=None, e_ops=[], store_states=False, t0=0, nout=1):
+    def evolve(self, rho0, dt, Nt, evecs=None, e_ops=[], store_states=False, t0=0, nout=1,
+               precision='fp64'):
         if self.R is None:
             self.redfield_tensor()
-        return _redfield(self.R, rho0, evecs=self.evecs, Nt=Nt, dt=dt, t0=t0, e_ops=e_ops)
+        return _redfield(self.R, rho0, evecs=self.evecs, Nt=Nt, dt=dt, t0=t0, e_ops=e_ops,
+                         store_states=True if precision == 'fp64' else store_states,
+                         precision=precision)
 
     def steady_state(self):
         pass
