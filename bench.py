@@ -53,6 +53,11 @@ def parse():
     p.add_argument('--no-cpu', action='store_true', help='skip the CPU baseline leg')
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-adjoint', action='store_true')
+    p.add_argument('--no-redfield', action='store_true')
+    p.add_argument('--redfield-only', action='store_true',
+                   help='run only the dense Redfield leg and print its JSON')
+    p.add_argument('--redfield-n', type=int, default=96)
+    p.add_argument('--redfield-rhs', type=int, default=512)
     return p.parse_args()
 
 
@@ -168,6 +173,12 @@ def gpu_arm(args, rank, world, local):
     lbuild.build()
     nat.require_device()
 
+    if args.redfield_only:
+        if rank == 0:
+            print(json.dumps(redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n,
+                                          n_rhs=args.redfield_rhs)))
+        return
+
     path = 'split' if args.path in ('auto', 'split') else 'fp64'
     K = args.steps if args.steps is not None else (FULL_STEPS if path == 'split' else 8)
     W = max(3, args.warmup)
@@ -221,6 +232,9 @@ def gpu_arm(args, rank, world, local):
     adj = None
     if not args.no_adjoint and rank == 0:
         adj = adjoint_leg(torch, dev)
+    red = None
+    if not args.no_redfield and rank == 0:
+        red = redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n, n_rhs=args.redfield_rhs)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -274,6 +288,7 @@ def gpu_arm(args, rank, world, local):
         'roofline': roof,
         'e2e': e2e,
         'adjoint': adj,
+        'redfield': red,
         'cpu_baseline': cpu,
     }
     if rank == 0:
@@ -349,6 +364,64 @@ def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=
                         % (N, batch, n_sites, n_sites - 1, n_sites, checkpoint),
             'sample_steps': steps, 'path': 'fp64',
             'forward_s': tf, 'adjoint_s': tb, 'adjoint_over_forward': tb / tf}
+
+
+def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k64=3):
+    """Dense Redfield workload: Liouville dim 9216, 512 initial density
+    matrices as one right-hand-side block (2000-step workload; a sample of
+    steps is timed).  Tensor-core split path vs the plain FP64 GPU path:
+    per-step time from the difference of two split runs (removes the
+    one-off operand conversion), FP64 from k64 steps, and the split error on
+    populations and final states over those k64 steps."""
+    from lime_gb300 import chains
+    from lime_gb300.redfield import redfield_tensor, propagate_vec, propagate_vec_split
+    w = chains.redfield_chain(n=n, n_rhs=n_rhs, cfg=5)
+    R, evecs = redfield_tensor(w['H'], w['a_ops'], w['spectra'], device=dev)
+    V = torch.as_tensor(evecs, dtype=torch.complex128, device=dev)
+    r0 = V.mH @ torch.as_tensor(w['rho0'], dtype=torch.complex128, device=dev) @ V
+    e_eb = [V.mH @ torch.as_tensor(e, dtype=torch.complex128, device=dev) @ V
+            for e in chains.population_ops(n)]
+    Rg = (R.R, n)
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b) / 1e3
+
+    propagate_vec_split(Rg, r0, dt, 1, e_eb)
+    _, t1 = timed(lambda: propagate_vec_split(Rg, r0, dt, k_split[0], e_eb))
+    _, t2 = timed(lambda: propagate_vec_split(Rg, r0, dt, k_split[1], e_eb))
+    per_step = (t2 - t1) / (k_split[1] - k_split[0])
+    (o64, _, r64), t64 = timed(lambda: propagate_vec(Rg, r0, dt, k64, e_eb))
+    (osp, _, rsp), _ = timed(lambda: propagate_vec_split(Rg, r0, dt, k64, e_eb))
+    D = n * n
+    stage_flop = 8.0 * D * D * n_rhs          # one complex D x D x R GEMM
+    issued = 5 * stage_flop                   # five fp16 products per real block
+    pk = peaks.get('bf16_tflops_sustained') or 1700.0
+    split_rate = n_rhs / per_step
+    fp64_rate = n_rhs * k64 / t64
+    return {'workload': 'Redfield dense superoperator, spin-boson-like exciton chain N=%d '
+                        '(Liouville dim %d), Ohmic bath, %d initial density matrices as one '
+                        'right-hand-side block' % (n, D, n_rhs),
+            'unit': 'instance-steps/s',
+            'split': {'value': split_rate, 'ms_per_step': per_step * 1e3,
+                      'sample': 'difference of %d- and %d-step runs' % k_split},
+            'fp64_gpu': {'value': fp64_rate, 'ms_per_step': t64 / k64 * 1e3,
+                         'sample': '%d RK4 steps' % k64},
+            'speedup_vs_fp64_gpu': split_rate / fp64_rate,
+            'split_max_population_error': (osp - o64).abs().max().item(),
+            'split_max_state_error': (rsp - r64).abs().max().item(),
+            'error_sample': 'all %d right-hand sides, %d steps' % (n_rhs, k64),
+            'roofline': {'bound': 'tensor', 'unit': 'TFLOP/s',
+                         'achieved_algorithmic': 4 * stage_flop / per_step / 1e12,
+                         'achieved_issued': 4 * issued / per_step / 1e12,
+                         'peak': pk, 'frac_issued': 4 * issued / per_step / 1e12 / pk,
+                         'note': 'per-step time includes the 4 stage launches and one '
+                                 'observable launch'}}
 
 
 def e2e_leg(wl, K, path, dev):

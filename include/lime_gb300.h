@@ -226,21 +226,27 @@ int lime_redfield_rk4_f64(const LimeRedfieldRK4Desc* d, void* stream);
 
 /* The same RK4 on the tcgen05 tensor cores in split precision: per stage
  * one GEMM [Yr|Yi] = [Lr|Li] . [[Sr,Si],[-Si,Sr]] with the operands streamed
- * by bulk copies from pre-tiled fp16 pieces (A = R: per-row 7-bit fixed
- * point + two fp16 residuals; B = stage input: 10-bit fixed point + fp16
- * residual), exact dominant product, fp32 two-sum accumulation, RK4 state
- * in fp32 hi + lo.  Replaces the same loop as lime_redfield_rk4_f64.
+ * by bulk copies from pre-tiled fp16 pieces (A = R, each row scaled by a
+ * power of two and split into a 7-bit fixed-point part + two fp16
+ * residuals; B = stage input: 10-bit fixed point + fp16 residual), exact
+ * dominant product, fp32 two-sum accumulation, RK4 state in fp32 hi + lo.
+ * Observables are a second GEMM of the same form (A = the observables,
+ * K split across CTAs, fp64 partial sums).  Replaces the same loop as
+ * lime_redfield_rk4_f64.
  *   R        [n^2][n^2] complex128 (from lime_redfield_build_f64)
  *   rho      [n_rhs][n^2] complex128 in/out, row-major vec(rho_r) per RHS
- *   scale_a_log2  R * 2^a with max |R| ~ 2^12
- *   scale_b_log2  rho * 2^b with max |rho| * 1.25 <= 2^13
+ *   scale_b_log2  rho * 2^b with max |rho(t)| * 2^b <= 2^13 at all times
+ *            (2^13 / (1.25 max |rho0|) for trace-preserving generators);
+ *            a state leaving that range raises LIME_FLAG_RANGE
  *   obs_ops  [n_obs][n][n]; obs_out [n_steps/obs_every][n_rhs][n_obs]
- *   workspace lime_redfield_split_workspace() bytes, 1024-byte aligned
+ *            (<E_o> = Tr(E_o rho) after steps obs_every, 2 obs_every, ...)
+ *   workspace lime_redfield_split_workspace(n, n_rhs, n_obs) bytes,
+ *            1024-byte aligned
  *   status   device int32 (LIME_FLAG_* bits)
  */
 typedef struct {
   int32_t n, n_rhs, n_steps, n_obs, obs_every;
-  int32_t scale_a_log2, scale_b_log2;
+  int32_t scale_b_log2;
   double dt;
   const double* R;
   double* rho;
@@ -250,7 +256,7 @@ typedef struct {
   int32_t* status;
 } LimeRedfieldSplitDesc;
 
-size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs);
+size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs, int32_t n_obs);
 int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* stream);
 
 /* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate

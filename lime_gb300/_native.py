@@ -124,7 +124,7 @@ class RedfieldRK4Desc(ctypes.Structure):
 
 class RedfieldSplitDesc(ctypes.Structure):
     _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('n_steps', c_int32), ('n_obs', c_int32),
-                ('obs_every', c_int32), ('scale_a_log2', c_int32), ('scale_b_log2', c_int32),
+                ('obs_every', c_int32), ('scale_b_log2', c_int32),
                 ('dt', c_double),
                 ('R', c_void_p), ('rho', c_void_p),
                 ('obs_ops', c_void_p), ('obs_out', c_void_p),
@@ -144,7 +144,7 @@ SIGNATURES = [
     ('lime_redfield_build_f64', c_int32, [ctypes.POINTER(RedfieldBuildDesc), c_void_p]),
     ('lime_redfield_rk4_f64_workspace', c_size_t, [c_int32, c_int32]),
     ('lime_redfield_rk4_f64', c_int32, [ctypes.POINTER(RedfieldRK4Desc), c_void_p]),
-    ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32]),
+    ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32, c_int32]),
     ('lime_redfield_rk4_split', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),

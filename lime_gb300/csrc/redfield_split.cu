@@ -72,15 +72,18 @@ __host__ __device__ __forceinline__ size_t piece_off(int KC, int n, int k) {
 }
 
 struct StageArgs {
-  int Dp, W, KC, NT, stage;          // W = 2 Rp output columns, KC = 2Dp / 64 chunks, NT = W / 128
-  float inv_scale, sb, magic_b, c_half, c_full, c_sixth, c_sixth_lo;
+  int Dp, W, KC, MT, NT, stage;      // W = 2 Rp output columns, KC = 2Dp / 64 chunks, NT = W / 128
+  int KS, pairs_per_split;           // observable pass: K split over KS CTAs, pairs of chunks each
+  float inv_sb, sb, magic_b, c_half, c_full, c_sixth, c_sixth_lo;
   const uint8_t* A[3];               // pre-tiled [MT][KC] blocks
+  const float* row_inv;              // per-row inverse operand scale (powers of two; 0 on padding)
   const uint8_t* Bc[2];              // current stage input pieces, pre-tiled [NT][KC]
   uint8_t* Bn[2];                    // next stage input pieces
   float* Phi;                        // [W][Dp]
   float* Plo;
   float* Acc;
-  int Rp;
+  int Rp, R, n_obs;
+  double* obs;                       // observable pass: [R][n_obs] complex, accumulated
   int32_t* status;
   uint32_t max_wait;
 };
@@ -163,12 +166,26 @@ __device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
 
 __device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory"); }
 
-__global__ void __launch_bounds__(kThreads, 1) stage_kernel(StageArgs a) {
+// kObserve = false: one RK4 stage, Y = L S over the full K, fused stage
+// update.  kObserve = true: observables <E_o> = sum_d Et[o][d] P[d][r] of
+// the state held in Bc, K split over KS CTAs whose fp64 partial sums are
+// added atomically into a.obs.
+template <bool kObserve>
+__global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
   extern __shared__ uint8_t smem_raw[];
   Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-  const int mt = blockIdx.x / a.NT, nt = blockIdx.x % a.NT;
-  const int KC = a.KC;
+  const int tile = kObserve ? (int)(blockIdx.x % (a.MT * a.NT)) : (int)blockIdx.x;
+  const int mt = tile / a.NT, nt = tile % a.NT;
+  int c0 = 0, KC = a.KC;                      // this CTA's chunk range [c0, c0 + KC)
+  if (kObserve) {
+    const int ks = blockIdx.x / (a.MT * a.NT);
+    const int p0 = ks * a.pairs_per_split;
+    const int p1 = min(p0 + a.pairs_per_split, a.KC >> 1);
+    c0 = 2 * p0;
+    KC = 2 * max(p1 - p0, 0);
+  }
+  const int KCall = a.KC;
 
   if (warp == 0) {
     tc::tmem_alloc(&S.tmem_base, kTmemCols);
@@ -203,8 +220,8 @@ __global__ void __launch_bounds__(kThreads, 1) stage_kernel(StageArgs a) {
         if (*(volatile int*)&S.abort) break;
         issued = c + 1;
         tc::mbar_arrive_expect_tx(&S.full[s], 5 * kPiece);
-        const size_t ao = ((size_t)mt * KC + c) * kPiece;
-        const size_t bo = ((size_t)nt * KC + c) * kPiece;
+        const size_t ao = ((size_t)mt * KCall + c0 + c) * kPiece;
+        const size_t bo = ((size_t)nt * KCall + c0 + c) * kPiece;
         tc::bulk_g2s(S.stage[s][0], a.A[0] + ao, kPiece, &S.full[s]);
         tc::bulk_g2s(S.stage[s][1], a.A[1] + ao, kPiece, &S.full[s]);
         tc::bulk_g2s(S.stage[s][2], a.A[2] + ao, kPiece, &S.full[s]);
@@ -304,10 +321,26 @@ __global__ void __launch_bounds__(kThreads, 1) stage_kernel(StageArgs a) {
     }
     // park the derivative tile in the ring: every MMA has completed once the
     // last accumulator pair was seen, so the tensor core reads no operand
+    const float rs = __fmul_rn(a.row_inv[mt * kBM + r], a.inv_sb);
+    if (kObserve) {
+      const int o = mt * kBM + r;
+      if (ok && o < a.n_obs && KC > 0) {
+        const double rsd = (double)rs;
+#pragma unroll
+        for (int c = 0; c < 64; ++c) {
+          const int jj = nt * kBN + 64 * h + c;
+          const int j = jj < a.Rp ? jj : jj - a.Rp;
+          if (j < a.R) {
+            const double f = ((double)hi[c] + (double)lo[c * kBM]) * rsd;
+            atomicAdd(a.obs + 2 * ((size_t)j * a.n_obs + o) + (jj < a.Rp ? 0 : 1), f);
+          }
+        }
+      }
+    } else {
     float* ft = reinterpret_cast<float*>(&S.stage[0][0][0]);
     if (ok) {
 #pragma unroll
-      for (int c = 0; c < 64; ++c) ft[(64 * h + c) * kFStride + r] = __fmul_rn(__fadd_rn(hi[c], lo[c * kBM]), a.inv_scale);
+      for (int c = 0; c < 64; ++c) ft[(64 * h + c) * kFStride + r] = __fmul_rn(__fadd_rn(hi[c], lo[c * kBM]), rs);
     }
     epi_bar();
     if (!*(volatile int*)&S.abort) {
@@ -375,6 +408,7 @@ __global__ void __launch_bounds__(kThreads, 1) stage_kernel(StageArgs a) {
       if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
       if (range) atomicOr(a.status, LIME_FLAG_RANGE);
     }
+    }
   }
 
   tc::tc_fence_before();
@@ -387,16 +421,27 @@ __global__ void __launch_bounds__(kThreads, 1) stage_kernel(StageArgs a) {
 }
 
 // ---------------------------------------------------------------- set-up kernels
-// A pieces of one row of [Lr | Li] (row = blockIdx.x), per-row 7-bit fixed point
-__global__ void convert_a_kernel(const double2* L, int D, int Dp, int KC, double sa, uint8_t* A0, uint8_t* A1,
-                                 uint8_t* A2) {
+// A pieces of one row (row = blockIdx.x) of [Mr | Mi]: the row is scaled by
+// the power of two that brings its largest component into [2^12, 2^13), then
+// split as A0 = 64 k (|k| <= 127) + fp16 residuals A1, A2; row_inv gets the
+// inverse scale (0 for padding rows and all-zero rows).  transposed = 0:
+// M = L (D x D, element (row, kk) = L[row][kk]); transposed = 1: M = the
+// observables, element (o, a n + b) = E_o[b][a], so that <E_o> = sum_d M[o][d]
+// vec(rho)[d].
+__global__ void convert_rows_kernel(const double2* M, int transposed, int n, int rows, int D, int Dp, int KC,
+                                    uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
   __shared__ double red[8];
   const int row = blockIdx.x;
+  auto elem = [&](int kk) -> double2 {
+    if (!transposed) return M[(size_t)row * D + kk];
+    const int ia = kk / n, ib = kk - ia * n;
+    return M[(size_t)row * D + (size_t)ib * n + ia];
+  };
   double mx = 0.0;
-  if (row < D)
+  if (row < rows)
     for (int k = threadIdx.x; k < D; k += blockDim.x) {
-      const double2 z = L[(size_t)row * D + k];
-      mx = fmax(mx, fmax(fabs(z.x), fabs(z.y)) * sa);
+      const double2 z = elem(k);
+      mx = fmax(mx, fmax(fabs(z.x), fabs(z.y)));
     }
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
@@ -408,24 +453,25 @@ __global__ void convert_a_kernel(const double2* L, int D, int Dp, int KC, double
   }
   __syncthreads();
   mx = red[0];
-  double q = 1.0, inv_q = 0.0;
-  if (mx >= 0x1p-18) {
-    const int e = ilogb(mx);
-    q = ldexp(1.0, e - 6);
-    inv_q = ldexp(1.0, 6 - e);
+  int sh = 0;
+  bool live = row < rows && mx > 0.0 && isfinite(mx);
+  if (live) {
+    sh = 12 - ilogb(mx);                 // mx * 2^sh in [2^12, 2^13)
+    if (sh > 140 || sh < -140) live = false;
   }
+  if (threadIdx.x == 0) row_inv[row] = live ? ldexpf(1.f, -sh) : 0.f;
   const int mt = row >> 7, rr = row & 127;
   for (int k = threadIdx.x; k < 2 * Dp; k += blockDim.x) {
     double x = 0.0;
-    if (row < D) {
+    if (live) {
       const int kk = k < Dp ? k : k - Dp;
       if (kk < D) {
-        const double2 z = L[(size_t)row * D + kk];
-        x = (k < Dp ? z.x : z.y) * sa;
+        const double2 z = elem(kk);
+        x = ldexp(k < Dp ? z.x : z.y, sh);
       }
     }
-    const double kq = fmin(fmax(rint(x * inv_q), -kA0Max), kA0Max);
-    const double v0 = kq * q;
+    const double kq = fmin(fmax(rint(x * (1.0 / 64.0)), -kA0Max), kA0Max);
+    const double v0 = kq * 64.0;
     const double r1 = x - v0;
     const __half h1 = __double2half(r1);
     const __half h2 = __double2half(r1 - (double)__half2float(h1));
@@ -467,26 +513,6 @@ __global__ void final_state_kernel(const float* Phi, const float* Plo, int Dp, i
   }
 }
 
-// obs[r][o] = sum_ab E_o[b][a] rho_r[a][b]: one block per (RHS, observable)
-__global__ void observe_kernel(const float* Phi, const float* Plo, int Dp, int Rp, int n, int n_obs,
-                               const double2* E, double2* out) {
-  const int D = n * n;
-  const int r = blockIdx.x / n_obs, o = blockIdx.x % n_obs;
-  double sr = 0.0, si = 0.0;
-  for (int d = threadIdx.x; d < D; d += blockDim.x) {
-    const int ia = d / n, ib = d - ia * n;
-    const double2 ev = E[(size_t)o * D + (size_t)ib * n + ia];
-    const size_t er = (size_t)r * Dp + d, ei = (size_t)(r + Rp) * Dp + d;
-    const double pr = (double)Phi[er] + (double)Plo[er], pi = (double)Phi[ei] + (double)Plo[ei];
-    sr += ev.x * pr - ev.y * pi;
-    si += ev.x * pi + ev.y * pr;
-  }
-  __shared__ double red[32];
-  sr = block_sum<128>(sr, red);
-  si = block_sum<128>(si, red);
-  if (threadIdx.x == 0) out[(size_t)r * n_obs + o] = make_double2(sr, si);
-}
-
 }  // namespace rsp
 }  // namespace lime
 
@@ -502,46 +528,75 @@ static void rsp_dims(int n, int R, int& D, int& Dp, int& Rp, int& W, int& KC, in
   NT = W / 128;
 }
 
-extern "C" size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs) {
-  if (n <= 0 || n_rhs <= 0) return 0;
+struct RspLayout {
+  size_t apiece, epiece, bpiece, state, rows;
+  size_t total;
+};
+
+static RspLayout rsp_layout(int n, int R, int n_obs) {
   int D, Dp, Rp, W, KC, MT, NT;
-  rsp_dims(n, n_rhs, D, Dp, Rp, W, KC, MT, NT);
-  const size_t a_bytes = 3 * (size_t)MT * KC * rsp::kPiece;
-  const size_t b_bytes = 4 * (size_t)NT * KC * rsp::kPiece;
-  const size_t s_bytes = 3 * (size_t)W * Dp * sizeof(float);
-  return a_bytes + b_bytes + s_bytes + 4096;
+  rsp_dims(n, R, D, Dp, Rp, W, KC, MT, NT);
+  const int MTo = n_obs > 0 ? (n_obs + 127) / 128 : 0;
+  RspLayout l;
+  l.apiece = (size_t)MT * KC * rsp::kPiece;
+  l.epiece = (size_t)MTo * KC * rsp::kPiece;
+  l.bpiece = (size_t)NT * KC * rsp::kPiece;
+  l.state = (size_t)W * Dp * sizeof(float);
+  l.rows = (size_t)(MT + MTo) * 128 * sizeof(float);
+  l.total = 3 * l.apiece + 3 * l.epiece + 4 * l.bpiece + 3 * l.state + ((l.rows + 1023) / 1024) * 1024 + 4096;
+  return l;
+}
+
+extern "C" size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs, int32_t n_obs) {
+  if (n <= 0 || n_rhs <= 0 || n_obs < 0) return 0;
+  return rsp_layout(n, n_rhs, n_obs).total;
 }
 
 extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* stream) {
   if (!d || d->n <= 0 || d->n_rhs <= 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
   if (!d->R || !d->rho || !d->workspace || !d->status) return LIME_ERR_ARG;
   if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
-  if (d->scale_a_log2 < -60 || d->scale_a_log2 > 60 || d->scale_b_log2 < -60 || d->scale_b_log2 > 60)
-    return LIME_ERR_ARG;
+  if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60) return LIME_ERR_ARG;
   if ((int64_t)d->n * d->n > (1 << 20)) return LIME_ERR_UNSUPPORTED;
-  if (d->workspace_bytes < lime_redfield_split_workspace(d->n, d->n_rhs)) return LIME_ERR_WORKSPACE;
+  if (d->workspace_bytes < lime_redfield_split_workspace(d->n, d->n_rhs, d->n_obs)) return LIME_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
   int D, Dp, Rp, W, KC, MT, NT;
   rsp_dims(d->n, d->n_rhs, D, Dp, Rp, W, KC, MT, NT);
+  const int MTo = d->n_obs > 0 ? (d->n_obs + 127) / 128 : 0;
+  const RspLayout L = rsp_layout(d->n, d->n_rhs, d->n_obs);
   cudaStream_t st = (cudaStream_t)stream;
   uint8_t* ws = reinterpret_cast<uint8_t*>(d->workspace);
-  const size_t apiece = (size_t)MT * KC * rsp::kPiece, bpiece = (size_t)NT * KC * rsp::kPiece;
-  uint8_t* A[3] = {ws, ws + apiece, ws + 2 * apiece};
-  uint8_t* B[4] = {ws + 3 * apiece, ws + 3 * apiece + bpiece, ws + 3 * apiece + 2 * bpiece,
-                   ws + 3 * apiece + 3 * bpiece};
-  float* Phi = reinterpret_cast<float*>(ws + 3 * apiece + 4 * bpiece);
+  uint8_t* A[3] = {ws, ws + L.apiece, ws + 2 * L.apiece};
+  uint8_t* Ep[3] = {ws + 3 * L.apiece, ws + 3 * L.apiece + L.epiece, ws + 3 * L.apiece + 2 * L.epiece};
+  uint8_t* bb = ws + 3 * L.apiece + 3 * L.epiece;
+  uint8_t* B[4] = {bb, bb + L.bpiece, bb + 2 * L.bpiece, bb + 3 * L.bpiece};
+  float* Phi = reinterpret_cast<float*>(bb + 4 * L.bpiece);
   float* Plo = Phi + (size_t)W * Dp;
   float* Acc = Plo + (size_t)W * Dp;
+  float* row_inv = Acc + (size_t)W * Dp;           // [MT*128] generator rows, then [MTo*128] observables
   int64_t launches = 0;
 
-  rsp::convert_a_kernel<<<Dp, 256, 0, st>>>(reinterpret_cast<const double2*>(d->R), D, Dp, KC,
-                                           ldexp(1.0, d->scale_a_log2), A[0], A[1], A[2]);
+  rsp::convert_rows_kernel<<<Dp, 256, 0, st>>>(reinterpret_cast<const double2*>(d->R), 0, d->n, D, D, Dp, KC,
+                                              A[0], A[1], A[2], row_inv);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
+  if (MTo > 0) {
+    rsp::convert_rows_kernel<<<MTo * 128, 256, 0, st>>>(reinterpret_cast<const double2*>(d->obs_ops), 1, d->n,
+                                                       d->n_obs, D, Dp, KC, Ep[0], Ep[1], Ep[2],
+                                                       row_inv + (size_t)MT * 128);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+    const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
+    const size_t slots = (size_t)(d->n_steps / obs_every);
+    if (slots > 0) {
+      LIME_CUDA_TRY(cudaMemsetAsync(d->obs_out, 0, slots * d->n_rhs * d->n_obs * 2 * sizeof(double), st));
+    }
+  }
 
   rsp::StageArgs a{};
-  a.Dp = Dp; a.W = W; a.KC = KC; a.NT = NT; a.Rp = Rp;
-  a.inv_scale = ldexpf(1.f, -(d->scale_a_log2 + d->scale_b_log2));
+  a.Dp = Dp; a.W = W; a.KC = KC; a.MT = MT; a.NT = NT; a.Rp = Rp; a.R = d->n_rhs;
+  a.KS = 1; a.pairs_per_split = KC / 2;
+  a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
   a.sb = ldexpf(1.f, d->scale_b_log2);
   a.magic_b = ldexpf(1.5f, 23 + 3);          // B0 quantum q_B = 2^3 (|B| <= 2^13)
   a.c_half = (float)(d->dt / 2.0);
@@ -549,6 +604,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   a.c_sixth = (float)(d->dt / 6.0);
   a.c_sixth_lo = (float)(d->dt / 6.0 - (double)a.c_sixth);
   a.A[0] = A[0]; a.A[1] = A[1]; a.A[2] = A[2];
+  a.row_inv = row_inv;
   a.Phi = Phi; a.Plo = Plo; a.Acc = Acc;
   a.status = d->status;
   a.max_wait = 1u << 26;
@@ -561,8 +617,30 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
 
+  // observable pass: same operands as a stage with A = observables, K split
+  // so that the grid covers the GPU about twice
+  rsp::StageArgs ao = a;
+  int n_sm = 148;
+  {
+    int dev = 0;
+    LIME_CUDA_TRY(cudaGetDevice(&dev));
+    LIME_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  if (MTo > 0) {
+    ao.MT = MTo;
+    ao.A[0] = Ep[0]; ao.A[1] = Ep[1]; ao.A[2] = Ep[2];
+    ao.row_inv = row_inv + (size_t)MT * 128;
+    ao.n_obs = d->n_obs;
+    const int pairs = KC / 2;
+    int ks = (2 * n_sm) / (MTo * NT);
+    ks = ks < 1 ? 1 : (ks > pairs ? pairs : ks);
+    ao.pairs_per_split = (pairs + ks - 1) / ks;
+    ao.KS = (pairs + ao.pairs_per_split - 1) / ao.pairs_per_split;
+  }
+
   const size_t smem = sizeof(rsp::Smem) + 1024;
-  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::stage_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
   int cur = 0;   // B[2cur], B[2cur+1] hold the current stage input
   for (int step = 0; step < d->n_steps; ++step) {
@@ -570,16 +648,17 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
       a.stage = s;
       a.Bc[0] = B[2 * cur]; a.Bc[1] = B[2 * cur + 1];
       a.Bn[0] = B[2 * (cur ^ 1)]; a.Bn[1] = B[2 * (cur ^ 1) + 1];
-      rsp::stage_kernel<<<MT * NT, rsp::kThreads, smem, st>>>(a);
+      rsp::gemm_kernel<false><<<MT * NT, rsp::kThreads, smem, st>>>(a);
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
       cur ^= 1;
     }
-    if (d->n_obs > 0 && ((step + 1) % obs_every) == 0) {
+    if (MTo > 0 && ((step + 1) % obs_every) == 0) {
+      // B[2cur], B[2cur+1] now hold the new state (the next step's stage-0 input)
       const int slot = (step + 1) / obs_every - 1;
-      rsp::observe_kernel<<<d->n_rhs * d->n_obs, 128, 0, st>>>(
-          Phi, Plo, Dp, Rp, d->n, d->n_obs, reinterpret_cast<const double2*>(d->obs_ops),
-          reinterpret_cast<double2*>(d->obs_out) + (size_t)slot * d->n_rhs * d->n_obs);
+      ao.Bc[0] = B[2 * cur]; ao.Bc[1] = B[2 * cur + 1];
+      ao.obs = d->obs_out + (size_t)slot * d->n_rhs * d->n_obs * 2;
+      rsp::gemm_kernel<true><<<ao.KS * MTo * NT, rsp::kThreads, smem, st>>>(ao);
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
     }

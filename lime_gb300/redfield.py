@@ -173,11 +173,11 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
     """Tensor-core split-precision RK4 (``lime_redfield_rk4_split``) of
     eigenbasis density matrices (B, n, n) under the dense generator.
 
-    Same returns as ``propagate_vec`` without states.  The generator is
-    scaled to max |R| ~ 2^12 and the states to max |rho0| * 1.25 <= 2^13
-    (powers of two, so the scaling is exact); a run whose states leave the
-    fixed-point range raises LIME_FLAG_RANGE and is repeated with the state
-    scale lowered by 4x.
+    Same returns as ``propagate_vec`` without states.  The states are
+    scaled to max |rho0| * 1.25 <= 2^13 (a power of two, so the scaling is
+    exact; the kernel scales every generator and observable row itself); a
+    run whose states leave the fixed-point range raises LIME_FLAG_RANGE and
+    is repeated with the state scale lowered by 4x.
     """
     lib = nat.require_device()
     Rd, n = R
@@ -190,12 +190,9 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
         E = torch.stack(list(e_eb)).to(CDT).contiguous()
         n_obs = E.shape[0]
     n_slots = n_steps // obs_every
-    rmax = float(torch.view_as_real(Rd).abs().max().item()) if Rd.numel() else 0.0
     pmax = float(torch.view_as_real(rho0_eb).abs().max().item()) if rho0_eb.numel() else 0.0
-    sa = _pow2_floor(4096.0 / rmax) if rmax > 0 else 0
     sb = _pow2_floor(8192.0 / (1.25 * pmax)) if pmax > 0 else 0
-    sa = max(-60, min(60, sa))
-    wsb = lib.lime_redfield_split_workspace(n, B)
+    wsb = lib.lime_redfield_split_workspace(n, B, n_obs)
     ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
     base = ws.data_ptr()
     aligned = (base + 1023) // 1024 * 1024
@@ -206,7 +203,7 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
         status.zero_()
         d = nat.RedfieldSplitDesc()
         d.n, d.n_rhs, d.n_steps, d.n_obs, d.obs_every = n, B, n_steps, n_obs, obs_every
-        d.scale_a_log2, d.scale_b_log2 = sa, max(-60, min(60, sb))
+        d.scale_b_log2 = max(-60, min(60, sb))
         d.dt = float(dt)
         d.R, d.rho = Rd.data_ptr(), P.data_ptr()
         if E is not None:

@@ -92,3 +92,18 @@ def test_split_launches_are_counted():
     torch.cuda.synchronize()
     # convert + init + 4 stages per step + final state
     assert _native.launch_count() - c0 == 3 + 4 * 10
+
+
+def test_split_many_observables():
+    """More than one 128-row tile of observables (general complex matrices)."""
+    from lime_gb300.redfield import redfield_tensor, _redfield
+    n = 12
+    w = chains.redfield_chain(n=n, n_rhs=3, cfg=5)
+    R, evecs = redfield_tensor(w['H'], w['a_ops'], w['spectra'])
+    rng = np.random.default_rng(7)
+    e_ops = list(rng.normal(size=(140, n, n)) + 1j * rng.normal(size=(140, n, n)))
+    ref = _redfield(R, w['rho0'], evecs=evecs, Nt=30, dt=0.05, e_ops=e_ops, store_states=False)
+    spl = _redfield(R, w['rho0'], evecs=evecs, Nt=30, dt=0.05, e_ops=e_ops, store_states=False,
+                    precision='split')
+    assert spl.observables.shape == (3, 30, 140)
+    assert rel(spl.observables, ref.observables) < TOL
