@@ -9,7 +9,7 @@
 // no-swizzle UMMA layout: every (128-row tile, 64-wide K chunk) block is one
 // contiguous 16 KB piece, moved by the bulk-copy (TMA) engine with
 // cp.async.bulk into a two-stage shared-memory ring and completed on
-// mbarriers.
+// mbarriers (two 64-K stages measured faster than four 32-K ones).
 //
 // Warp roles per CTA (one 128 x 128 output tile, 320 threads, 1 CTA/SM):
 //   warp 0      producer: bulk copies of 5 pieces per K chunk (80 KB)
@@ -42,12 +42,14 @@
 namespace lime {
 namespace rsp {
 
-constexpr int kBM = 128, kBN = 128;   // output tile; K advances in chunks of 64
-constexpr uint32_t kPiece = 16384;                 // 128 x 64 fp16
+constexpr int kBM = 128, kBN = 128;   // output tile
+constexpr int kCK = 64;                            // K per chunk (one ring stage)
+constexpr int kGroup = 128 / kCK;                  // chunks per exactly accumulated 128 K
+constexpr uint32_t kPiece = 128 * kCK * 2;         // 128 x 64 fp16 = 16 KB
 constexpr int kStages = 2;
 constexpr int kThreads = 320;
 constexpr int kEpiThreads = 256;
-constexpr uint32_t kLBO = 128, kSBO = 1024;        // canonical K-major block strides (bytes)
+constexpr uint32_t kLBO = 128, kSBO = kCK * 16;    // canonical K-major block strides (bytes)
 constexpr uint32_t kTmemCols = 512;
 constexpr double kA0Max = 127.0;
 constexpr float kBMax = 8192.f;                    // |B| bound of the 10-bit fixed point (q_B = 8)
@@ -62,18 +64,18 @@ struct __align__(1024) Smem {
 };
 static_assert((size_t)kBN * kFStride * sizeof(float) <= sizeof(Smem::stage), "derivative tile fits the ring");
 
-// byte offset of (row, k) inside one 128 x 64 block
+// byte offset of (row, k) inside one 128 x kCK block
 __host__ __device__ __forceinline__ uint32_t blk_off(int row, int k) {
   return (uint32_t)(row >> 3) * kSBO + (uint32_t)(k >> 3) * kLBO + (uint32_t)(row & 7) * 16u +
          (uint32_t)(k & 7) * 2u;
 }
 __host__ __device__ __forceinline__ size_t piece_off(int KC, int n, int k) {
-  return ((size_t)(n >> 7) * KC + (k >> 6)) * kPiece + blk_off(n & 127, k & 63);
+  return ((size_t)(n >> 7) * KC + k / kCK) * kPiece + blk_off(n & 127, k % kCK);
 }
 
 struct StageArgs {
-  int Dp, W, KC, MT, NT, stage;      // W = 2 Rp output columns, KC = 2Dp / 64 chunks, NT = W / 128
-  int KS, pairs_per_split;           // observable pass: K split over KS CTAs, pairs of chunks each
+  int Dp, W, KC, MT, NT, stage;      // W = 2 Rp output columns, KC = 2Dp / kCK chunks, NT = W / 128
+  int KS, groups_per_split;          // observable pass: K split over KS CTAs, 128-K groups each
   float inv_sb, sb, magic_b, c_half, c_full, c_sixth, c_sixth_lo;
   const uint8_t* A[3];               // pre-tiled [MT][KC] blocks
   const float* row_inv;              // per-row inverse operand scale (powers of two; 0 on padding)
@@ -180,10 +182,10 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
   int c0 = 0, KC = a.KC;                      // this CTA's chunk range [c0, c0 + KC)
   if (kObserve) {
     const int ks = blockIdx.x / (a.MT * a.NT);
-    const int p0 = ks * a.pairs_per_split;
-    const int p1 = min(p0 + a.pairs_per_split, a.KC >> 1);
-    c0 = 2 * p0;
-    KC = 2 * max(p1 - p0, 0);
+    const int g0 = ks * a.groups_per_split;
+    const int g1 = min(g0 + a.groups_per_split, a.KC / kGroup);
+    c0 = kGroup * g0;
+    KC = kGroup * max(g1 - g0, 0);
   }
   const int KCall = a.KC;
 
@@ -214,8 +216,8 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
     if (lane == 0) {
       int issued = 0;
       for (int c = 0; c < KC; ++c) {
-        const int s = c & 1;
-        const uint32_t ph = (uint32_t)(c >> 1) & 1u;
+        const int s = c % kStages;
+        const uint32_t ph = (uint32_t)(c / kStages) & 1u;
         if (!tc::mbar_wait_bounded(&S.empty[s], ph ^ 1u, a.max_wait)) { atomicExch(&S.abort, 1); break; }
         if (*(volatile int*)&S.abort) break;
         issued = c + 1;
@@ -228,19 +230,20 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
         tc::bulk_g2s(S.stage[s][3], a.Bc[0] + bo, kPiece, &S.full[s]);
         tc::bulk_g2s(S.stage[s][4], a.Bc[1] + bo, kPiece, &S.full[s]);
       }
-      // the copies of the last (up to two) issued chunks have landed before exit
+      // the copies of the last (up to kStages) issued chunks have landed before exit
       for (int c = issued - 1; c >= 0 && c >= issued - kStages; --c)
-        tc::mbar_wait_bounded(&S.full[c & 1], (uint32_t)(c >> 1) & 1u, a.max_wait);
+        tc::mbar_wait_bounded(&S.full[c % kStages], (uint32_t)(c / kStages) & 1u, a.max_wait);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer
     if (lane == 0) {
       constexpr uint32_t idesc = tc::idesc_f16(kBM, kBN, 0);
       for (int c = 0; c < KC; ++c) {
-        const int s = c & 1;
-        const uint32_t ph = (uint32_t)(c >> 1) & 1u;
-        const int p = c >> 1, b = p & 1;
-        const bool first = (c & 1) == 0;
+        const int s = c % kStages;
+        const uint32_t ph = (uint32_t)(c / kStages) & 1u;
+        const int p = c / kGroup, b = p & 1;
+        const bool first = (c % kGroup) == 0;
+        const bool last = (c % kGroup) == kGroup - 1;
         if (!tc::mbar_wait_bounded(&S.full[s], ph, a.max_wait)) { atomicExch(&S.abort, 1); break; }
         if (first && !tc::mbar_wait_bounded(&S.acce[b], ((uint32_t)(p >> 1) & 1u) ^ 1u, a.max_wait)) {
           atomicExch(&S.abort, 1);
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
         const uint32_t d1 = d0 + 128u;
         const uint32_t base = tc::smem_u32(S.stage[s][0]);
 #pragma unroll
-        for (int ks = 0; ks < 4; ++ks) {
+        for (int ks = 0; ks < kCK / 16; ++ks) {
           const uint32_t ko = (uint32_t)ks * 2u * kLBO;
           const uint64_t a0 = tc::smem_desc_noswizzle(base + 0 * kPiece + ko, kLBO, kSBO);
           const uint64_t a1 = tc::smem_desc_noswizzle(base + 1 * kPiece + ko, kLBO, kSBO);
@@ -267,7 +270,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
           tc::mma_f16_ss(d1, a2, b0, idesc, 1u);
         }
         tc::mma_commit(&S.empty[s]);
-        if (!first) tc::mma_commit(&S.accf[b]);
+        if (last) tc::mma_commit(&S.accf[b]);
       }
       // every MMA this thread issued has completed before TMEM is released
       tc::mma_commit(&S.drain);
@@ -285,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
     float* lo = S.lo + (64 * h) * kBM + r;
 #pragma unroll
     for (int c = 0; c < 64; ++c) { hi[c] = 0.f; lo[c * kBM] = 0.f; }
-    const int n_pairs = KC >> 1;
+    const int n_pairs = KC / kGroup;
     bool ok = true;
     for (int p = 0; p < n_pairs; ++p) {
       const int b = p & 1;
@@ -298,6 +301,8 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(StageArgs a) {
       const uint32_t d0 = lane_addr + (uint32_t)(2 * b) * 128u + 64u * h;
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
+        // (one load and wait per accumulator measured faster than both loads
+        // under one wait)
         float v[16], er[16];
         tc::tmem_ld16(d0 + 16 * q, v);
 #pragma unroll
@@ -475,7 +480,7 @@ __global__ void convert_rows_kernel(const double2* M, int transposed, int n, int
     const double r1 = x - v0;
     const __half h1 = __double2half(r1);
     const __half h2 = __double2half(r1 - (double)__half2float(h1));
-    const size_t off = ((size_t)mt * KC + (k >> 6)) * kPiece + blk_off(rr, k & 63);
+    const size_t off = ((size_t)mt * KC + k / kCK) * kPiece + blk_off(rr, k % kCK);
     *reinterpret_cast<__half*>(A0 + off) = __double2half(v0);
     *reinterpret_cast<__half*>(A1 + off) = h1;
     *reinterpret_cast<__half*>(A2 + off) = h2;
@@ -523,7 +528,7 @@ static void rsp_dims(int n, int R, int& D, int& Dp, int& Rp, int& W, int& KC, in
   Dp = (D + 127) / 128 * 128;
   Rp = (R + 63) / 64 * 64;
   W = 2 * Rp;
-  KC = 2 * Dp / 64;
+  KC = 2 * Dp / rsp::kCK;
   MT = Dp / 128;
   NT = W / 128;
 }
@@ -595,7 +600,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
 
   rsp::StageArgs a{};
   a.Dp = Dp; a.W = W; a.KC = KC; a.MT = MT; a.NT = NT; a.Rp = Rp; a.R = d->n_rhs;
-  a.KS = 1; a.pairs_per_split = KC / 2;
+  a.KS = 1; a.groups_per_split = KC / rsp::kGroup;
   a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
   a.sb = ldexpf(1.f, d->scale_b_log2);
   a.magic_b = ldexpf(1.5f, 23 + 3);          // B0 quantum q_B = 2^3 (|B| <= 2^13)
@@ -631,11 +636,11 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
     ao.A[0] = Ep[0]; ao.A[1] = Ep[1]; ao.A[2] = Ep[2];
     ao.row_inv = row_inv + (size_t)MT * 128;
     ao.n_obs = d->n_obs;
-    const int pairs = KC / 2;
+    const int groups = KC / rsp::kGroup;
     int ks = (2 * n_sm) / (MTo * NT);
-    ks = ks < 1 ? 1 : (ks > pairs ? pairs : ks);
-    ao.pairs_per_split = (pairs + ks - 1) / ks;
-    ao.KS = (pairs + ao.pairs_per_split - 1) / ao.pairs_per_split;
+    ks = ks < 1 ? 1 : (ks > groups ? groups : ks);
+    ao.groups_per_split = (groups + ks - 1) / ks;
+    ao.KS = (groups + ao.groups_per_split - 1) / ao.groups_per_split;
   }
 
   const size_t smem = sizeof(rsp::Smem) + 1024;
