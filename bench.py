@@ -54,6 +54,7 @@ def parse():
     p.add_argument('--no-e2e', action='store_true')
     p.add_argument('--no-adjoint', action='store_true')
     p.add_argument('--no-redfield', action='store_true')
+    p.add_argument('--no-ragged', action='store_true')
     p.add_argument('--redfield-only', action='store_true',
                    help='run only the dense Redfield leg and print its JSON')
     p.add_argument('--redfield-n', type=int, default=96)
@@ -235,6 +236,9 @@ def gpu_arm(args, rank, world, local):
     red = None
     if not args.no_redfield and rank == 0:
         red = redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n, n_rhs=args.redfield_rhs)
+    rag = None
+    if not args.no_ragged and rank == 0:
+        rag = ragged_leg(torch, dev)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -289,6 +293,7 @@ def gpu_arm(args, rank, world, local):
         'e2e': e2e,
         'adjoint': adj,
         'redfield': red,
+        'uneven_batch': rag,
         'cpu_baseline': cpu,
     }
     if rank == 0:
@@ -422,6 +427,32 @@ def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k
                          'peak': pk, 'frac_issued': 4 * issued / per_step / 1e12 / pk,
                          'note': 'per-step time includes the 4 stage launches and one '
                                  'observable launch'}}
+
+
+def ragged_leg(torch, dev, batch=1024, steps=2):
+    """Uneven batch: 1024 chains with N uniform over {8..256}, three dense
+    complex collapse operators each (2000-step workload; a sample of steps
+    is timed), through the public uneven-batch API: every size group is one
+    batched FP64 launch, the groups run concurrently on their own streams.
+    Dense collapse operators are outside the tensor-core kernel, so this is
+    the FP64 rate."""
+    from lime_gb300 import chains, engine
+    w = chains.uneven_batch(batch=batch, n_steps=steps)
+    ns = w['ns']
+    E = [[chains.population_ops(int(n))[0]] for n in ns]
+    engine.propagate_ragged(w['H'], w['rho0'], w['dt'], 1, w['c_ops'], E)   # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    engine.propagate_ragged(w['H'], w['rho0'], w['dt'], steps, w['c_ops'], E)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    flop = float(sum(256.0 * int(n) ** 3 for n in ns)) * steps   # 64 (1 + K) N^3, K = 3
+    return {'workload': 'uneven batch: %d chains, N uniform over {8,16,32,64,128,256}, '
+                        'tridiagonal + 0.01 GOE, 3 dense complex collapse operators' % len(ns),
+            'path': 'fp64 (one batched launch per size, groups on concurrent streams)',
+            'unit': 'instance-steps/s', 'value': len(ns) * steps / t, 'steps': steps,
+            'wall_s_incl_setup': t, 'algorithmic_tflops': flop / t / 1e12,
+            'note': 'wall time of the public call, including generator preparation'}
 
 
 def e2e_leg(wl, K, path, dev):

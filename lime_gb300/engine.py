@@ -301,20 +301,12 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
     return obs_out[:, :, :n_obs], None, status
 
 
-def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
-              states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
-              check: bool = True, obs_every: int = 1, events=None, drive=None):
-    """RK4-propagate density matrices under ``gen``.
-
-    ``rho0``: (n, n) or (B, n, n); with a non-shared generator B must equal
-    ``gen.P``.  Returns ``(obs, states, rho)`` device tensors:
-    ``obs`` (B, n_steps // obs_every, n_obs) = Tr(E rho) after steps
-    obs_every-1, 2 obs_every-1, ..., ``states`` (B, n_steps // states_every,
-    n, n) or None, ``rho`` (B, n, n) final.  ``events``: optional pair of
-    CUDA events recorded on the launching stream around the kernel call.
-    ``drive``: optional (ops (q, n, n), coef (n_steps, q) float64) device
-    tensors for H(t) = H0 - sum_q coef[k, q] ops[q] during step k (FP64 path).
-    """
+def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
+            states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
+            obs_every: int = 1, events=None, drive=None):
+    """Enqueue one propagation on the current stream; returns a closure that
+    checks the status word (synchronising the stream) and assembles
+    ``(obs, states, rho)``."""
     if obs_every < 1 or states_every < 0 or n_steps < 0:
         raise ValueError('obs_every must be >= 1, states_every >= 0, n_steps >= 0')
     device = gen.heff.device
@@ -354,12 +346,108 @@ def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
                                   param_batch=B, events=events)
     else:
         raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
-    if check:
-        flags = int(status.item())
-        if flags:
-            raise nat.KernelFlagError(flags, 'lindblad RK4 (%s)' % precision)
-    if not herm:
-        o = o[:B] + 1j * o[B:]
-        s = None if s is None else s[:B] + 1j * s[B:]
-        work = work[:B] + 1j * work[B:]
-    return o, s, work
+
+    def finish(check: bool = True):
+        if check:
+            flags = int(status.item())
+            if flags:
+                raise nat.KernelFlagError(flags, 'lindblad RK4 (%s)' % precision)
+        if not herm:
+            return (o[:B] + 1j * o[B:], None if s is None else s[:B] + 1j * s[B:],
+                    work[:B] + 1j * work[B:])
+        return o, s, work
+
+    return finish
+
+
+def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
+              states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
+              check: bool = True, obs_every: int = 1, events=None, drive=None):
+    """RK4-propagate density matrices under ``gen``.
+
+    ``rho0``: (n, n) or (B, n, n); with a non-shared generator B must equal
+    ``gen.P``.  Returns ``(obs, states, rho)`` device tensors:
+    ``obs`` (B, n_steps // obs_every, n_obs) = Tr(E rho) after steps
+    obs_every-1, 2 obs_every-1, ..., ``states`` (B, n_steps // states_every,
+    n, n) or None, ``rho`` (B, n, n) final.  ``events``: optional pair of
+    CUDA events recorded on the launching stream around the kernel call.
+    ``drive``: optional (ops (q, n, n), coef (n_steps, q) float64) device
+    tensors for H(t) = H0 - sum_q coef[k, q] ops[q] during step k (FP64 path).
+    """
+    return _launch(gen, rho0, dt, n_steps, e_ops, states_every, precision, trace_tol,
+                   obs_every, events, drive)(check)
+
+
+def _dims(a):
+    if isinstance(a, torch.Tensor):
+        return a.dim()
+    return np.ndim(a.toarray() if hasattr(a, 'toarray') else a)
+
+
+def is_ragged(H) -> bool:
+    """True for an uneven batch: a list/tuple of two or more 2-D Hamiltonians
+    (the reference's list form [H0, [H1, f1], ...] is the driven solver)."""
+    return isinstance(H, (list, tuple)) and len(H) >= 2 and all(
+        not isinstance(x, (list, tuple)) and _dims(x) == 2 for x in H)
+
+
+def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None,
+                     e_ops_list=None, states_every: int = 0, precision: str = 'fp64',
+                     trace_tol: float | None = None, obs_every: int = 1, device=None):
+    """Uneven batch: instance i has its own Hamiltonian H_list[i] (n_i x n_i),
+    collapse operators c_ops_list[i] and observables e_ops_list[i] (lists of
+    n_i x n_i operators; every instance has the same number of observables).
+
+    Instances with equal dimension and operator counts are stacked into one
+    batched launch; the launches of different dimensions run concurrently on
+    separate CUDA streams and the status words are checked once all are
+    enqueued.  ``precision``: 'fp64', 'split' (every group must be
+    tensor-core capable) or 'auto' (split where ``split_supported``, FP64
+    elsewhere).  Returns three lists in input order: observables
+    (n_steps // obs_every, n_obs), states or None, final rho.
+    """
+    B = len(H_list)
+    if len(rho0_list) != B:
+        raise ValueError('%d Hamiltonians but %d initial states' % (B, len(rho0_list)))
+    c_ops_list = [[] for _ in range(B)] if c_ops_list is None else list(c_ops_list)
+    e_ops_list = [[] for _ in range(B)] if e_ops_list is None else list(e_ops_list)
+    if len(c_ops_list) != B or len(e_ops_list) != B:
+        raise ValueError('c_ops_list and e_ops_list need one entry per instance')
+    n_obs = {len(e) for e in e_ops_list}
+    if len(n_obs) > 1:
+        raise ValueError('every instance needs the same number of observables')
+    device = _dev(device)
+    groups = {}
+    for i in range(B):
+        h = H_list[i]
+        n = int(h.shape[-1]) if hasattr(h, 'shape') else int(np.shape(h)[-1])
+        key = (n, len(c_ops_list[i]))
+        groups.setdefault(key, []).append(i)
+    main = torch.cuda.current_stream(device)
+    pending = []
+    for (n, K), idx in sorted(groups.items()):
+        st = torch.cuda.Stream(device=device)
+        st.wait_stream(main)
+        with torch.cuda.stream(st):
+            H = torch.stack([as_device(H_list[i], device) for i in idx])
+            ops = [torch.stack([as_device(c_ops_list[i][k], device) for i in idx]) for k in range(K)]
+            gen = LindbladGenerator.build(H, ops, device=device)
+            prec = precision
+            if precision == 'auto':
+                prec = 'split' if split_supported(gen) is None else 'fp64'
+            rho = torch.stack([as_device(rho0_list[i], device) for i in idx])
+            E = [torch.stack([as_device(e_ops_list[i][o], device) for i in idx])
+                 for o in range(len(e_ops_list[idx[0]]))]
+            fin = _launch(gen, rho, dt, n_steps, E, states_every=states_every, precision=prec,
+                          trace_tol=trace_tol, obs_every=obs_every)
+        pending.append((idx, st, fin))
+    obs, states, rhos = [None] * B, [None] * B, [None] * B
+    for idx, st, fin in pending:
+        main.wait_stream(st)
+        with torch.cuda.stream(st):
+            o, s, r = fin(True)
+        for j, i in enumerate(idx):
+            obs[i] = o[j]
+            states[i] = None if s is None else s[j]
+            rhos[i] = r[j]
+    return obs, states, rhos

@@ -9,7 +9,10 @@ Same names, arguments, return values and side-effect files as the reference
 * ``liouvillian`` / ``lindbladian`` (single RHS evaluations) lime/oqs.py:706-723
 
 Beyond the reference: a leading batch axis on ``H`` / ``rho0`` (and on each
-collapse operator) propagates many instances in one launch.
+collapse operator) propagates many instances in one launch, and a list of
+Hamiltonians of different dimensions (an uneven batch, with per-instance
+lists of initial states, collapse operators and observables) propagates
+every size group concurrently and returns one ``Result`` per instance.
 
 Errors follow the reference: ValueError for wrong operator counts
 (lime/oqs.py:1310,1326), TypeError for non-Hermitian bath operators.  There is
@@ -54,6 +57,8 @@ def _lindblad(H, rho0, c_ops, e_ops=None, Nt=1, dt=0.005, return_result=True,
     ``nout`` steps), ``store_states=False`` (keep only the final state) and
     ``precision``.
     """
+    if engine.is_ragged(H):
+        return _lindblad_ragged(H, rho0, c_ops, e_ops, Nt, dt, precision, store_states, nout)
     e_ops = [] if e_ops is None else list(e_ops)
     batched = _is_batched(H, rho0) or any(
         isinstance(c, engine.DiagonalOps) and np.ndim(c.l) == 3 for c in (c_ops or []))
@@ -87,6 +92,28 @@ def _lindblad(H, rho0, c_ops, e_ops=None, Nt=1, dt=0.005, return_result=True,
             t += dt
             f.write(fmt.format(t, *ob[k]))
     return _squeeze_batch(_np(rho), batched)
+
+
+def _lindblad_ragged(H, rho0, c_ops, e_ops, Nt, dt, precision, store_states, nout):
+    """Uneven batch (a list of Hamiltonians of different dimensions): one
+    ``Result`` per instance, in input order.  ``rho0``, ``c_ops`` and
+    ``e_ops`` are lists with one entry per instance (``c_ops[i]`` and
+    ``e_ops[i]`` lists of operators of instance i's dimension)."""
+    B = len(H)
+    if not isinstance(rho0, (list, tuple)) or len(rho0) != B:
+        raise ValueError('an uneven batch needs one initial state per Hamiltonian')
+    c_ops = [[] for _ in range(B)] if c_ops is None else c_ops
+    e_ops = [[] for _ in range(B)] if e_ops is None else e_ops
+    obs, states, rhos = engine.propagate_ragged(
+        list(H), list(rho0), dt, Nt, c_ops_list=c_ops, e_ops_list=e_ops,
+        states_every=nout if store_states else 0, precision=precision, obs_every=nout)
+    out = []
+    for i in range(B):
+        res = Result(dt=dt, Nt=Nt, rho0=rho0[i], t0=0.0, nout=nout)
+        res.observables = _np(obs[i])
+        res.rholist = list(_np(states[i])) if states[i] is not None else [_np(rhos[i])]
+        out.append(res)
+    return out
 
 
 def _correlation_2p_1t(H, rho0, ops, c_ops, dt, Nt, method='lindblad', output='cor.dat',
@@ -175,7 +202,7 @@ class Lindblad_solver:
 
     def evolve(self, rho0, dt, Nt, t0=0., e_ops=None, return_result=True, nout=1,
                store_states=True):
-        if isinstance(self.H, list):
+        if isinstance(self.H, list) and not engine.is_ragged(self.H):
             from .driven import _lindblad_driven
             return _lindblad_driven(self.H, rho0=rho0, c_ops=self.c_ops, e_ops=e_ops,
                                     Nt=Nt, dt=dt, t0=t0)
