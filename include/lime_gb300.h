@@ -259,6 +259,47 @@ typedef struct {
 size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs, int32_t n_obs);
 int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* stream);
 
+/* ------------------------------------------------------------------ */
+/* General Lindblad RK4 on the tensor cores (split precision)           */
+/* ------------------------------------------------------------------ */
+
+/* Any dimension, dense collapse operators: per RK4 stage two streaming
+ * tcgen05 GEMMs per instance, [X; Y_1..Y_K] = [Heff; L_1..L_K] rho_s and
+ * Z = [L_1 | .. | L_K] [Y_1^dag; ..; Y_K^dag] = sum_k L_k rho_s L_k^dag,
+ * with the split-precision operands of lime_redfield_rk4_split, then
+ * f = Z - i(X - X^dag) + M o rho_s and the RK4 update fused into the second
+ * GEMM's epilogue.  Replaces the same loops as lime_lindblad_rk4_f64 for
+ * Hermitian rho (run a non-Hermitian start as its two Hermitian parts).
+ *   rho       [B][n][n] complex128 in/out
+ *   heff      [P|1][n][n] (lime_lindblad_prepare_f64), stride heff_stride
+ *   m         [P|1][n][n] or NULL (diagonal collapse operators), m_stride
+ *   l_ops     [P|1][n_ops][n][n] dense collapse operators or NULL, l_stride
+ *   obs_ops   [P|1][n_obs][n][n], obs_stride; obs_out [B][n_steps/obs_every][n_obs]
+ *             Tr(E rho) after steps obs_every, 2 obs_every, ...
+ *   scale_b_log2  rho * 2^b, max |rho(t)| 2^b <= 2^13
+ *   scale_y_log2  (L_k rho) * 2^y, max |L_k rho(t)| 2^y <= 2^13
+ *             (a value out of range raises LIME_FLAG_RANGE)
+ *   workspace lime_lindblad_stream_workspace(n, batch, G, n_ops) bytes,
+ *             1024-byte aligned; G = 1 when heff and l_ops are shared
+ *             (strides 0), else param_batch
+ */
+typedef struct {
+  int32_t n, batch, param_batch, n_ops, n_steps, n_obs, obs_every;
+  int32_t scale_b_log2, scale_y_log2;
+  double dt;
+  double* rho;
+  const double* heff;     int64_t heff_stride;
+  const double* m;        int64_t m_stride;
+  const double* l_ops;    int64_t l_stride;
+  const double* obs_ops;  int64_t obs_stride;
+  double* obs_out;
+  void* workspace;        size_t workspace_bytes;
+  int32_t* status;
+} LimeLindbladStreamDesc;
+
+size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops);
+int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream);
+
 /* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate
  * device memory: a host framework whose pool owns the GPU, a latency-critical
  * loop where cudaMalloc/cudaFree would synchronise the device, or a process

@@ -51,6 +51,25 @@ __device__ __forceinline__ double block_sum(double v, double* red) {
   return s;
 }
 
+// ---------------------------------------------------------------- compensated RK4 update
+// Final RK4 combination x += (acc + f) dt/6 on an fp32 pair (x, lo): dt/6 is
+// the float pair c6 + c6lo, the increment's rounding error and the sum's
+// two-sum error are carried in lo, so neither rounding nor the step size
+// drifts over thousands of steps (lime/phys.py:636-649).
+__device__ __forceinline__ float rk4_final_f32(float x, float acc, float f, float c6, float c6lo, float& lo) {
+  const float ksum = __fadd_rn(acc, f);
+  const float inc = __fmul_rn(ksum, c6);
+  const float inc_res = __fmaf_rn(ksum, c6, -inc);
+  const float inc_lo = __fmaf_rn(ksum, c6lo, inc_res);
+  const float sum = __fadd_rn(x, inc);
+  const float bv = __fsub_rn(sum, x);
+  const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(sum, bv)), __fsub_rn(inc, bv));
+  float l = __fadd_rn(lo, __fadd_rn(err, inc_lo));
+  const float hi2 = __fadd_rn(sum, l);
+  lo = __fsub_rn(l, __fsub_rn(hi2, sum));
+  return hi2;
+}
+
 }  // namespace lime
 
 #define LIME_CUDA_TRY(expr)                            \

@@ -168,21 +168,6 @@ __device__ __forceinline__ bool mma_pass(uint32_t tbase, uint32_t b0_addr, uint3
   return tc::mbar_wait_bounded(mbar, parity, max_wait);
 }
 
-// Two-sum update of (hi, lo) += (acc + f) dt/6 with dt/6 = c6 + c6lo.
-__device__ __forceinline__ float rk4_final(float x, float accj, float f, float c6, float c6lo, float& lo) {
-  const float ksum = __fadd_rn(accj, f);
-  const float inc = __fmul_rn(ksum, c6);
-  const float inc_res = __fmaf_rn(ksum, c6, -inc);
-  const float inc_lo = __fmaf_rn(ksum, c6lo, inc_res);
-  const float sum = __fadd_rn(x, inc);
-  const float bv = __fsub_rn(sum, x);
-  const float err = __fadd_rn(__fsub_rn(x, __fsub_rn(sum, bv)), __fsub_rn(inc, bv));
-  float l = __fadd_rn(lo, __fadd_rn(err, inc_lo));
-  const float hi2 = __fadd_rn(sum, l);
-  lo = __fsub_rn(l, __fsub_rn(hi2, sum));
-  return hi2;
-}
-
 __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a) {
   extern __shared__ uint8_t smem_raw[];
   Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -363,7 +348,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
             rs_d_next = __fmaf_rn(cst, fd, rho_d);
           } else {
             lo_d = S.rlo[i * 128 + r];
-            rho_d = rk4_final(rho_d, acc_d, fd, a.c_sixth, a.c_sixth_lo, lo_d);
+            rho_d = rk4_final_f32(rho_d, acc_d, fd, a.c_sixth, a.c_sixth_lo, lo_d);
             rs_d_next = rho_d;
           }
         }
@@ -387,7 +372,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
               nxt[e] = __fmaf_rn(cst, f, rho[jj]);
             } else {
               float lo = S.rlo[(j0 + jj) * 128 + r];
-              rho[jj] = rk4_final(rho[jj], acc[jj], f, a.c_sixth, a.c_sixth_lo, lo);
+              rho[jj] = rk4_final_f32(rho[jj], acc[jj], f, a.c_sixth, a.c_sixth_lo, lo);
               S.rlo[(j0 + jj) * 128 + r] = lo;
               nxt[e] = rho[jj];
             }

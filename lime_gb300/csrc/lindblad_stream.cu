@@ -1,0 +1,477 @@
+// General Lindblad RK4 on the sm_103a tensor cores: any dimension, dense
+// collapse operators, split precision (the streaming tile of
+// stream_gemm.cuh).
+//
+// Generator (lime/oqs.py:706-723, written with Heff = H - i/2 sum L^dag L):
+//     f(rho) = -i (X - X^dag) + sum_k L_k rho L_k^dag + M o rho,   X = Heff rho
+// per RK4 stage, for every instance, as two GEMMs of the real block form
+// [Yr | Yi] = [Ar | Ai] . [[Sr, Si], [-Si, Sr]]:
+//   GEMM 1   [X; Y_1; ...; Y_K] = [Heff; L_1; ...; L_K] . rho_s
+//            (A constant: converted once; B = the stage input rho_s)
+//   GEMM 2   Z = [L_1 | ... | L_K] . [Y_1^dag; ...; Y_K^dag] = sum_k L_k rho_s L_k^dag
+//            (A constant; B = Y^dag, written by GEMM 1's epilogue)
+// GEMM 2's epilogue assembles f = Z - i(X - X^dag) + M o rho_s (X from
+// GEMM 1, transposed reads through L2) and runs the RK4 stage update; with
+// no dense operator a plain kernel does the same without Z.  rho_s is
+// Hermitian (a non-Hermitian start runs as its two Hermitian parts), which
+// is what makes rho_s X^dag-free and Z = Z^dag.
+//
+// Layouts per instance (n padded to np, a multiple of 64; W = 2 np): state
+// hi, lo, RK4 accumulator, X and the stage input fp32 planar [W][np] with
+// element [comp * np + x][y] = comp-part of rho[y][x]; operands pre-tiled
+// in 16 KB pieces (piece_off).
+
+#include "stream_gemm.cuh"
+
+namespace lime {
+namespace lsm {
+
+using sg::kBM;
+using sg::kBN;
+using sg::kFStride;
+using sg::kPiece;
+
+struct Args {
+  int n, np, W, NT, K, P, G;          // G = generator sets (1 = shared)
+  int KC1, KC2, MT1, MT2;
+  float sb, inv_sb, sy, inv_sy;
+  sg::RK4 rk;
+  const uint8_t* A1[3];               // [G][MT1][KC1] pieces
+  const uint8_t* A2[3];               // [G][MT2][KC2] pieces
+  const float* rinv1;                 // [G][MT1 * 128]
+  const float* rinv2;                 // [G][MT2 * 128]
+  const uint8_t* B1c[2];              // [B][NT][KC1] current stage input
+  uint8_t* B1n[2];                    // next stage input
+  uint8_t* B2[2];                     // [B][NT][KC2]  Y^dag
+  float* Xg;                          // [B][W][np]
+  const float* Sc;                    // [B][W][np] current stage input (M term)
+  float* Sn;                          // next stage input
+  float* Phi;                         // [B][W][np]
+  float* Plo;
+  float* Acc;
+  const double2* m;                   // [P|1][n][n] or null
+  int64_t m_stride;
+  int32_t* status;
+  uint32_t max_wait;
+};
+
+__device__ __forceinline__ size_t inst_floats(const Args& a) { return (size_t)a.W * a.np; }
+
+// f for 8 rows y..y+7 of state column jj of instance b: Z (or 0) + the X
+// terms + the M term, in place.
+__device__ __forceinline__ void assemble_f(const Args& a, int b, int jj, int y, float (&f)[8]) {
+  const int np = a.np;
+  const bool im = jj >= np;
+  const int x = im ? jj - np : jj;
+  const float* X = a.Xg + (size_t)b * inst_floats(a);
+  float u[8];
+  if (!im) {
+    // Re f = Xi[y][x] + Xi[x][y]
+    sg::ld8(X + (size_t)(np + x) * np + y, u);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fadd_rn(u[i], X[(size_t)(np + y + i) * np + x]));
+  } else {
+    // Im f = Xr[x][y] - Xr[y][x]
+    sg::ld8(X + (size_t)x * np + y, u);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fsub_rn(X[(size_t)(y + i) * np + x], u[i]));
+  }
+  if (a.m != nullptr && x < a.n) {
+    const double2* M = a.m + (a.m_stride ? (int64_t)(b % a.P) * a.m_stride : 0);
+    const float* S = a.Sc + (size_t)b * inst_floats(a);
+    float sr[8], si[8];
+    sg::ld8(S + (size_t)x * np + y, sr);
+    sg::ld8(S + (size_t)(np + x) * np + y, si);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (y + i < a.n) {
+        const double2 mv = M[(size_t)(y + i) * a.n + x];
+        const float mr = (float)mv.x, mi = (float)mv.y;
+        f[i] = im ? __fmaf_rn(mr, si[i], __fmaf_rn(mi, sr[i], f[i]))
+                  : __fmaf_rn(mr, sr[i], __fmaf_rn(-mi, si[i], f[i]));
+      }
+    }
+  }
+}
+
+// RK4 stage update of 8 state rows and the next stage input (B1 pieces and,
+// for the M term, the fp32 copy).
+__device__ __forceinline__ void update8(const Args& a, int b, int jj, int y, const float (&f)[8], bool& bad,
+                                        bool& range) {
+  const size_t base = (size_t)b * inst_floats(a);
+  float sv[8];
+  sg::rk4_stage8(a.rk, a.Phi + base, a.Plo + base, a.Acc + base, (size_t)jj * a.np + y, f, sv, bad);
+  if (a.m != nullptr) sg::st8(a.Sn + base + (size_t)jj * a.np + y, sv);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    sv[i] = __fmul_rn(sv[i], a.sb);
+    range |= !(fabsf(sv[i]) <= sg::kBMax);
+  }
+  const bool im = jj >= a.np;
+  const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
+  sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, im ? jj - a.np : jj, im, sv);
+}
+
+// kZ = false: GEMM 1 (X and Y_k rows); kZ = true: GEMM 2 and the stage update.
+template <bool kZ>
+__global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
+  extern __shared__ uint8_t smem_raw[];
+  sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int t = threadIdx.x, lane = t & 31;
+  const int MT = kZ ? a.MT2 : a.MT1;
+  const int KC = kZ ? a.KC2 : a.KC1;
+  const int b = blockIdx.x / (MT * a.NT);
+  const int tile = blockIdx.x % (MT * a.NT);
+  const int mt = tile / a.NT, nt = tile % a.NT;
+  const int g = a.G == 1 ? 0 : b % a.P;
+  sg::setup(S);
+  sg::Tile T;
+  const size_t aoff = ((size_t)g * MT + mt) * KC * kPiece;
+  const size_t boff = ((size_t)b * a.NT + nt) * KC * kPiece;
+  for (int i = 0; i < 3; ++i) T.A[i] = (kZ ? a.A2[i] : a.A1[i]) + aoff;
+  for (int i = 0; i < 2; ++i) T.B[i] = (kZ ? a.B2[i] : a.B1c[i]) + boff;
+  T.c0 = 0;
+  T.n_chunks = KC;
+  T.row_inv = (kZ ? a.rinv2 : a.rinv1) + ((size_t)g * MT + mt) * kBM;
+  T.inv_sb = kZ ? a.inv_sy : a.inv_sb;
+  T.max_wait = a.max_wait;
+  const float* ft = S.tile();
+  if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
+    const int u = t - sg::kEpiFirst, ew = u >> 5;
+    const int np = a.np;
+    bool bad = false, range = false;
+    if (!kZ) {
+      // ---- X rows (block 0): the tile columns into Xg, runs of 8 rows
+      const int nlo = lane & 7, glo = lane >> 3;
+#pragma unroll 1
+      for (int it = 0; it < 8; ++it) {
+        const int wi = it * 8 + ew;
+        const int jl = (wi >> 2) * 8 + nlo;
+        const int dl = ((wi & 3) * 4 + glo) * 8;
+        const int R = mt * kBM + dl;
+        if (R < np) {
+          float v[8];
+          sg::ld8(ft + jl * kFStride + dl, v);
+          sg::st8(a.Xg + (size_t)b * inst_floats(a) + (size_t)(nt * kBN + jl) * np + R, v);
+        }
+      }
+      // ---- Y_k rows (blocks 1..K): Y^dag into B2, runs of 8 columns of one row
+      const int r = u & 127, o0 = u >> 7;
+      const int R = mt * kBM + r;
+      const int blk = R / np, yrow = R - blk * np;
+      if (blk >= 1 && blk <= a.K) {
+        uint8_t* B20 = a.B2[0] + (size_t)b * a.NT * a.KC2 * kPiece;
+        uint8_t* B21 = a.B2[1] + (size_t)b * a.NT * a.KC2 * kPiece;
+#pragma unroll 1
+        for (int i = 0; i < 8; ++i) {
+          const int cl = 8 * (o0 + 2 * i);
+          const int jj = nt * kBN + cl;
+          const bool im = jj >= np;
+          const int x = im ? jj - np : jj;
+          float v[8];
+#pragma unroll
+          for (int e = 0; e < 8; ++e) {
+            // S2[(k-1) np + x][yrow] = conj(Y_k[yrow][x]): real part Yr, imaginary part -Yi
+            const float y = ft[(cl + e) * kFStride + r];
+            v[e] = __fmul_rn(im ? -y : y, a.sy);
+            range |= !(fabsf(v[e]) <= sg::kBMax);
+          }
+          sg::scatter_cplx8(B20, B21, a.KC2, a.K * np, np, (blk - 1) * np + x, yrow, im, v);
+        }
+      }
+    } else {
+      // ---- f = Z + X terms + M term and the RK4 stage update, runs of 8 rows
+      const int nlo = lane & 7, glo = lane >> 3;
+#pragma unroll 1
+      for (int it = 0; it < 8; ++it) {
+        const int wi = it * 8 + ew;
+        const int jl = (wi >> 2) * 8 + nlo;
+        const int dl = ((wi & 3) * 4 + glo) * 8;
+        const int y = mt * kBM + dl, jj = nt * kBN + jl;
+        if (y < np) {
+          float f[8];
+          sg::ld8(ft + jl * kFStride + dl, f);
+          assemble_f(a, b, jj, y, f);
+          update8(a, b, jj, y, f, bad, range);
+        }
+      }
+    }
+    if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
+    if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+  }
+  sg::teardown(S, a.status);
+}
+
+// The stage update without dense operators (no GEMM 2): one thread per run
+// of 8 rows of one state column.
+__global__ void finish_kernel(Args a, int batch) {
+  const size_t runs = (size_t)a.W * (a.np / 8);
+  const size_t total = (size_t)batch * runs;
+  bool bad = false, range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / runs);
+    const int rem = (int)(q % runs);
+    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
+    float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    assemble_f(a, b, jj, y, f);
+    update8(a, b, jj, y, f, bad, range);
+  }
+  if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// A pieces: GEMM 1 rows (R = blk np + y: Heff for blk 0, L_blk otherwise)
+// and GEMM 2 rows (y: [L_1 | ... | L_K] row y).  One block per row.
+__global__ void convert_kernel(const double2* heff, int64_t heff_stride, const double2* l_ops, int64_t l_stride,
+                               Args a) {
+  const int rows1 = a.MT1 * kBM, rows2 = a.MT2 * kBM;
+  const int per_g = rows1 + (a.K > 0 ? rows2 : 0);
+  const int g = blockIdx.x / per_g;
+  const int q = blockIdx.x % per_g;
+  const int n = a.n, np = a.np;
+  if (q < rows1) {
+    const int R = q, blk = R / np, y = R - blk * np;
+    const bool valid = blk <= a.K && y < n;
+    const double2* src = blk == 0 ? heff + (heff_stride ? (int64_t)g * heff_stride : 0)
+                                  : l_ops + (l_stride ? (int64_t)g * l_stride : 0) + (int64_t)(blk - 1) * n * n;
+    auto elem = [&](int kk) -> double2 {
+      return kk < n ? src[(int64_t)y * n + kk] : make_double2(0.0, 0.0);
+    };
+    const size_t go = (size_t)g * a.MT1 * a.KC1 * kPiece;
+    sg::convert_row(elem, R, valid, np, np, a.KC1, const_cast<uint8_t*>(a.A1[0]) + go,
+                    const_cast<uint8_t*>(a.A1[1]) + go, const_cast<uint8_t*>(a.A1[2]) + go,
+                    const_cast<float*>(a.rinv1) + (size_t)g * rows1);
+  } else {
+    const int y = q - rows1;
+    const double2* src = l_ops + (l_stride ? (int64_t)g * l_stride : 0);
+    auto elem = [&](int kk) -> double2 {
+      const int k = kk / np, x = kk - k * np;
+      return x < n ? src[(int64_t)k * n * n + (int64_t)y * n + x] : make_double2(0.0, 0.0);
+    };
+    const size_t go = (size_t)g * a.MT2 * a.KC2 * kPiece;
+    sg::convert_row(elem, y, y < n, a.K * np, a.K * np, a.KC2, const_cast<uint8_t*>(a.A2[0]) + go,
+                    const_cast<uint8_t*>(a.A2[1]) + go, const_cast<uint8_t*>(a.A2[2]) + go,
+                    const_cast<float*>(a.rinv2) + (size_t)g * rows2);
+  }
+}
+
+// state, stage-input copy and first B1 from rho0 [B][n][n]
+__global__ void init_kernel(Args a, const double2* rho, int batch) {
+  const size_t runs = (size_t)a.W * (a.np / 8);
+  const size_t total = (size_t)batch * runs;
+  bool range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / runs);
+    const int rem = (int)(q % runs);
+    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
+    const bool im = jj >= a.np;
+    const int x = im ? jj - a.np : jj;
+    float hv[8], lv[8], sv[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      double v = 0.0;
+      if (x < a.n && y + i < a.n) {
+        const double2 z = rho[((size_t)b * a.n + y + i) * a.n + x];
+        v = im ? z.y : z.x;
+      }
+      hv[i] = (float)v;
+      lv[i] = (float)(v - (double)hv[i]);
+      sv[i] = __fmul_rn(hv[i], a.sb);
+      range |= !(fabsf(sv[i]) <= sg::kBMax);
+    }
+    const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
+    sg::st8(a.Phi + e, hv);
+    sg::st8(a.Plo + e, lv);
+    if (a.m != nullptr) sg::st8(a.Sn + e, hv);
+    const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
+    sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, x, im, sv);
+  }
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// obs[b][slot][o] = Tr(E_o rho_b) = sum_xy E_o[x][y] rho[y][x], fp64 from hi + lo
+__global__ void observe_kernel(Args a, const double2* E, int64_t e_stride, int n_obs, double2* out, int n_slots,
+                               int slot) {
+  const int b = blockIdx.x / n_obs, o = blockIdx.x % n_obs;
+  const double2* Eo = E + (e_stride ? (int64_t)(b % a.P) * e_stride : 0) + (int64_t)o * a.n * a.n;
+  const size_t base = (size_t)b * inst_floats(a);
+  double sr = 0.0, si = 0.0;
+  for (int q = threadIdx.x; q < a.n * a.n; q += blockDim.x) {
+    const int x = q / a.n, y = q - x * a.n;
+    const double2 ev = Eo[(size_t)x * a.n + y];
+    const size_t er = base + (size_t)x * a.np + y, ei = base + (size_t)(a.np + x) * a.np + y;
+    const double pr = (double)a.Phi[er] + (double)a.Plo[er];
+    const double pi = (double)a.Phi[ei] + (double)a.Plo[ei];
+    sr += ev.x * pr - ev.y * pi;
+    si += ev.x * pi + ev.y * pr;
+  }
+  __shared__ double red[32];
+  sr = block_sum<128>(sr, red);
+  si = block_sum<128>(si, red);
+  if (threadIdx.x == 0) out[((size_t)b * n_slots + slot) * n_obs + o] = make_double2(sr, si);
+}
+
+__global__ void final_kernel(Args a, double2* rho, int batch) {
+  const size_t total = (size_t)batch * a.n * a.n;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / ((size_t)a.n * a.n));
+    const int rem = (int)(q % ((size_t)a.n * a.n));
+    const int y = rem / a.n, x = rem - y * a.n;
+    const size_t base = (size_t)b * inst_floats(a);
+    const size_t er = base + (size_t)x * a.np + y, ei = base + (size_t)(a.np + x) * a.np + y;
+    rho[q] = make_double2((double)a.Phi[er] + (double)a.Plo[er], (double)a.Phi[ei] + (double)a.Plo[ei]);
+  }
+}
+
+}  // namespace lsm
+}  // namespace lime
+
+using namespace lime;
+
+namespace {
+
+struct LsmLayout {
+  int np, W, NT, KC1, KC2, MT1, MT2, G;
+  size_t a1, a2, r1, r2, b1, b2, st;   // bytes of one piece set / array
+  size_t total;
+};
+
+LsmLayout lsm_layout(int n, int batch, int G, int K) {
+  LsmLayout l;
+  l.np = (n + 63) / 64 * 64;
+  l.W = 2 * l.np;
+  l.NT = l.W / 128;
+  l.KC1 = 2 * l.np / sg::kCK;
+  l.KC2 = 2 * K * l.np / sg::kCK;
+  l.MT1 = ((1 + K) * l.np + 127) / 128;
+  l.MT2 = K > 0 ? (l.np + 127) / 128 : 0;
+  l.G = G;
+  l.a1 = (size_t)G * l.MT1 * l.KC1 * sg::kPiece;
+  l.a2 = (size_t)G * l.MT2 * l.KC2 * sg::kPiece;
+  l.r1 = ((size_t)G * l.MT1 * 128 * sizeof(float) + 1023) / 1024 * 1024;
+  l.r2 = ((size_t)G * l.MT2 * 128 * sizeof(float) + 1023) / 1024 * 1024;
+  l.b1 = (size_t)batch * l.NT * l.KC1 * sg::kPiece;
+  l.b2 = (size_t)batch * l.NT * l.KC2 * sg::kPiece;
+  l.st = (size_t)batch * l.W * l.np * sizeof(float);
+  // A1 x3, A2 x3, row scales, B1 x2 pieces x2 buffers, B2 x2 pieces,
+  // X, stage input x2, Phi, Plo, Acc
+  l.total = 3 * l.a1 + 3 * l.a2 + l.r1 + l.r2 + 4 * l.b1 + 2 * l.b2 + 6 * l.st + 4096;
+  return l;
+}
+
+int lsm_generators(int P, int64_t heff_stride, int K, int64_t l_stride) {
+  return (heff_stride == 0 && (K == 0 || l_stride == 0)) ? 1 : P;
+}
+
+}  // namespace
+
+extern "C" size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops) {
+  if (n <= 0 || batch <= 0 || n_generators <= 0 || n_ops < 0) return 0;
+  return lsm_layout(n, batch, n_generators, n_ops).total;
+}
+
+extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream) {
+  if (!d || d->n <= 0 || d->batch <= 0 || d->n_ops < 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (!d->rho || !d->heff || !d->workspace || !d->status) return LIME_ERR_ARG;
+  if (d->n_ops > 0 && !d->l_ops) return LIME_ERR_ARG;
+  if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
+  if (d->heff_stride < 0 || d->l_stride < 0 || d->m_stride < 0 || d->obs_stride < 0) return LIME_ERR_ARG;
+  if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60 || d->scale_y_log2 < -60 || d->scale_y_log2 > 60)
+    return LIME_ERR_ARG;
+  if (d->n > 4096 || d->n_ops > 64) return LIME_ERR_UNSUPPORTED;
+  const int P = d->param_batch > 0 ? d->param_batch : d->batch;
+  if (P > d->batch) return LIME_ERR_ARG;
+  if (!(d->dt == d->dt)) return LIME_ERR_ARG;
+  const int K = d->n_ops;
+  const int G = lsm_generators(P, d->heff_stride, K, d->l_stride);
+  const LsmLayout L = lsm_layout(d->n, d->batch, G, K);
+  if (d->workspace_bytes < L.total) return LIME_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
+  const int B = d->batch;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
+  lsm::Args a{};
+  a.n = d->n; a.np = L.np; a.W = L.W; a.NT = L.NT; a.K = K; a.P = P; a.G = G;
+  a.KC1 = L.KC1; a.KC2 = L.KC2; a.MT1 = L.MT1; a.MT2 = L.MT2;
+  for (int i = 0; i < 3; ++i) { a.A1[i] = w; w += L.a1; }
+  for (int i = 0; i < 3; ++i) { a.A2[i] = w; w += L.a2; }
+  a.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
+  a.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
+  uint8_t* B1[2][2];
+  for (int bb = 0; bb < 2; ++bb)
+    for (int i = 0; i < 2; ++i) { B1[bb][i] = w; w += L.b1; }
+  for (int i = 0; i < 2; ++i) { a.B2[i] = w; w += L.b2; }
+  a.Xg = reinterpret_cast<float*>(w); w += L.st;
+  float* Sbuf[2];
+  for (int i = 0; i < 2; ++i) { Sbuf[i] = reinterpret_cast<float*>(w); w += L.st; }
+  a.Phi = reinterpret_cast<float*>(w); w += L.st;
+  a.Plo = reinterpret_cast<float*>(w); w += L.st;
+  a.Acc = reinterpret_cast<float*>(w); w += L.st;
+  a.sb = ldexpf(1.f, d->scale_b_log2);
+  a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
+  a.sy = ldexpf(1.f, d->scale_y_log2);
+  a.inv_sy = ldexpf(1.f, -d->scale_y_log2);
+  a.rk = sg::RK4{0, (float)(d->dt / 2.0), (float)d->dt, (float)(d->dt / 6.0),
+                 (float)(d->dt / 6.0 - (double)(float)(d->dt / 6.0))};
+  a.m = reinterpret_cast<const double2*>(d->m);
+  a.m_stride = d->m_stride;
+  a.status = d->status;
+  a.max_wait = 1u << 26;
+  int64_t launches = 0;
+
+  const int per_g = L.MT1 * 128 + (K > 0 ? L.MT2 * 128 : 0);
+  lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
+                                                  reinterpret_cast<const double2*>(d->l_ops), d->l_stride, a);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  a.B1n[0] = B1[0][0]; a.B1n[1] = B1[0][1];
+  a.Sn = Sbuf[0];
+  const size_t runs = (size_t)B * L.W * (L.np / 8);
+  const int eb = (int)((runs + 255) / 256 < 65535 ? (runs + 255) / 256 : 65535);
+  lsm::init_kernel<<<eb, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->rho), B);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+
+  const size_t smem = sg::kSmemBytes;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  const int n_slots = d->n_steps / obs_every;
+  int cur = 0;
+  for (int step = 0; step < d->n_steps; ++step) {
+    for (int s = 0; s < 4; ++s) {
+      a.rk.stage = s;
+      a.B1c[0] = B1[cur][0]; a.B1c[1] = B1[cur][1];
+      a.B1n[0] = B1[cur ^ 1][0]; a.B1n[1] = B1[cur ^ 1][1];
+      a.Sc = Sbuf[cur];
+      a.Sn = Sbuf[cur ^ 1];
+      lsm::gemm_kernel<false><<<B * L.MT1 * L.NT, sg::kThreads, smem, st>>>(a);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+      if (K > 0) {
+        lsm::gemm_kernel<true><<<B * L.MT2 * L.NT, sg::kThreads, smem, st>>>(a);
+      } else {
+        lsm::finish_kernel<<<eb, 256, 0, st>>>(a, B);
+      }
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+      cur ^= 1;
+    }
+    if (d->n_obs > 0 && ((step + 1) % obs_every) == 0) {
+      lsm::observe_kernel<<<B * d->n_obs, 128, 0, st>>>(a, reinterpret_cast<const double2*>(d->obs_ops),
+                                                        d->obs_stride, d->n_obs,
+                                                        reinterpret_cast<double2*>(d->obs_out), n_slots,
+                                                        (step + 1) / obs_every - 1);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+    }
+  }
+  const size_t tot = (size_t)B * d->n * d->n;
+  const int fb = (int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535);
+  lsm::final_kernel<<<fb, 256, 0, st>>>(a, reinterpret_cast<double2*>(d->rho), B);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  count_launch(launches);
+  return LIME_OK;
+}

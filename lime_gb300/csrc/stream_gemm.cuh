@@ -1,0 +1,414 @@
+// Streaming split-precision GEMM tile on the sm_103a tensor cores (tcgen05),
+// shared by the dense Redfield RK4 and the general (dense collapse operator)
+// Lindblad RK4.
+//
+// One CTA computes one 128 x 128 fp32 tile of the real product C = A . B
+// where both operands live in global memory pre-tiled in the canonical
+// K-major, no-swizzle UMMA layout: every (128-row tile, 64-wide K chunk)
+// block is one contiguous 16 KB piece (blk_off), moved by the bulk-copy
+// (TMA) engine with cp.async.bulk into a two-stage shared-memory ring and
+// completed on mbarriers (two 64-K stages measured faster than four 32-K
+// ones).
+//
+// Warp roles (320 threads, 1 CTA/SM):
+//   warp 0      producer: bulk copies of 5 pieces per K chunk (80 KB)
+//   warp 1      MMA issuer: tcgen05.mma M=128 N=128 K=16, kind::f16
+//   warps 2..9  epilogue: drain TMEM accumulators into fp32 two-sum
+//               accumulators (hi words in registers, lo words in shared
+//               memory), then park the finished tile in shared memory for
+//               the caller's fused epilogue.
+//
+// Precision.  A = A0 (per-row 7-bit fixed point, 64 k with |k| <= 127 after
+// the row's power-of-two scaling) + A1 + A2 (fp16 residuals); B = B0
+// (10-bit fixed point, quantum 8 after the operand's power-of-two scaling)
+// + B1 (fp16 residual).  A tcgen05.mma rounds its fp32 result toward zero,
+// so the dominant product A0.B0 is kept exact: it is accumulated over 128 K
+// (integer multiples of 512 below 2^24) in its own TMEM accumulator D0, the
+// small products A1.B0 + A0.B1 + A1.B1 + A2.B0 in D1; every 128 K D0 enters
+// an fp32 two-sum (hi, lo) and D1 is added to lo, round to nearest.  TMEM:
+// D0/D1 double buffered, 4 x 128 = 512 columns, so the MMAs of the next
+// 128 K overlap the promotion of the previous ones.
+#pragma once
+
+#include "common.cuh"
+#include "tc_ptx.cuh"
+
+namespace lime {
+namespace sg {
+
+constexpr int kBM = 128, kBN = 128;                // output tile
+constexpr int kCK = 64;                            // K per chunk (one ring stage)
+constexpr int kGroup = 128 / kCK;                  // chunks per exactly accumulated 128 K
+constexpr uint32_t kPiece = 128 * kCK * 2;         // 128 x 64 fp16 = 16 KB
+constexpr int kStages = 2;
+constexpr int kThreads = 320;
+constexpr int kEpiThreads = 256;
+constexpr int kEpiFirst = 64;                      // first epilogue thread
+constexpr uint32_t kLBO = 128, kSBO = kCK * 16;    // canonical K-major block strides (bytes)
+constexpr uint32_t kTmemCols = 512;
+constexpr double kA0Max = 127.0;
+constexpr float kBMax = 8192.f;                    // |B| bound of the 10-bit fixed point (quantum 8)
+constexpr float kMagicB = 1.5f * 8388608.f * 8.f;  // 1.5 * 2^23 * 8: (x + M) - M rounds x to a multiple of 8
+constexpr int kFStride = kBN + 4;                  // padded column of the parked tile (floats)
+
+struct __align__(1024) Smem {
+  uint8_t stage[kStages][5][kPiece];               // A0 A1 A2 B0 B1; the parked tile after the last MMA
+  float lo[kBN * kBM];                             // low words of the fp32 two-sum accumulators, [col][row]
+  uint64_t full[kStages], empty[kStages], accf[2], acce[2], drain;
+  uint32_t tmem_base;
+  int abort;
+  __device__ float* tile() { return reinterpret_cast<float*>(&stage[0][0][0]); }   // [col][row], stride kFStride
+};
+static_assert((size_t)kBN * kFStride * sizeof(float) <= sizeof(Smem::stage), "parked tile fits the ring");
+constexpr size_t kSmemBytes = sizeof(Smem) + 1024;
+
+// byte offset of (row, k) inside one 128 x kCK block
+__host__ __device__ __forceinline__ uint32_t blk_off(int row, int k) {
+  return (uint32_t)(row >> 3) * kSBO + (uint32_t)(k >> 3) * kLBO + (uint32_t)(row & 7) * 16u +
+         (uint32_t)(k & 7) * 2u;
+}
+// byte offset of (row, k) in an operand of KC chunks per 128-row tile
+__host__ __device__ __forceinline__ size_t piece_off(int KC, int row, int k) {
+  return ((size_t)(row >> 7) * KC + k / kCK) * kPiece + blk_off(row & 127, k % kCK);
+}
+
+// x (scaled) = v0 (multiple of 8) + v1
+__device__ __forceinline__ void split_b(float x, float& v0, float& v1) {
+  v0 = __fsub_rn(__fadd_rn(x, kMagicB), kMagicB);
+  v1 = __fsub_rn(x, v0);
+}
+
+// 8 scaled B values at (row n, k..k+7), k % 8 == 0, as two 16-byte stores
+// per piece; `neg` stores their negatives.
+__device__ __forceinline__ void store_b8(uint8_t* B0, uint8_t* B1, int KC, int n, int k, const float (&x)[8],
+                                         bool neg) {
+  uint32_t h0[4], h1[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float a0, a1, b0, b1;
+    split_b(x[2 * i], a0, a1);
+    split_b(x[2 * i + 1], b0, b1);
+    const __half2 p = __floats2half2_rn(a0, b0);
+    const __half2 q = __floats2half2_rn(a1, b1);
+    h0[i] = *reinterpret_cast<const uint32_t*>(&p);
+    h1[i] = *reinterpret_cast<const uint32_t*>(&q);
+  }
+  const uint32_t sg = neg ? 0x80008000u : 0u;
+  const size_t off = piece_off(KC, n, k);
+  *reinterpret_cast<uint4*>(B0 + off) = make_uint4(h0[0] ^ sg, h0[1] ^ sg, h0[2] ^ sg, h0[3] ^ sg);
+  *reinterpret_cast<uint4*>(B1 + off) = make_uint4(h1[0] ^ sg, h1[1] ^ sg, h1[2] ^ sg, h1[3] ^ sg);
+}
+
+// Complex matrix S (K x N) into the real block operand [[Sr, Si], [-Si, Sr]]
+// (2K x 2N), stored transposed (B^T rows = the 2N output columns, K-major):
+// 8 consecutive rows k..k+7 of column j of S, real (im = false) or
+// imaginary parts, scaled.  Kp, Np: padded K and N (row/column offsets of
+// the second block).
+__device__ __forceinline__ void scatter_cplx8(uint8_t* B0, uint8_t* B1, int KC, int Kp, int Np, int k, int j,
+                                              bool im, const float (&x)[8]) {
+  if (!im) {
+    store_b8(B0, B1, KC, j, k, x, false);             // Sr at (k, j)
+    store_b8(B0, B1, KC, j + Np, Kp + k, x, false);   // Sr at (K + k, N + j)
+  } else {
+    store_b8(B0, B1, KC, j, Kp + k, x, true);         // -Si at (K + k, j)
+    store_b8(B0, B1, KC, j + Np, k, x, false);        // Si at (k, N + j)
+  }
+}
+
+__device__ __forceinline__ void ld8(const float* p, float (&v)[8]) {
+  const float4 x = *reinterpret_cast<const float4*>(p);
+  const float4 y = *reinterpret_cast<const float4*>(p + 4);
+  v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w; v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
+}
+__device__ __forceinline__ void st8(float* p, const float (&v)[8]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  *reinterpret_cast<float4*>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+
+// RK4 constants of one stage
+struct RK4 {
+  int stage;                                      // 0..3
+  float c_half, c_full, c_sixth, c_sixth_lo;      // dt/2, dt, dt/6 = c_sixth + c_sixth_lo
+};
+
+// One RK4 stage (lime/phys.py:636-649) for 8 state elements at e..e+7 of
+// the planar fp32 state (Phi + Plo, accumulator Acc) with derivative f:
+// writes the next stage input to sv (the new state after stage 3).
+__device__ __forceinline__ void rk4_stage8(const RK4& k, float* Phi, float* Plo, float* Acc, size_t e,
+                                           const float (&f)[8], float (&sv)[8], bool& bad) {
+  float ph[8];
+  ld8(Phi + e, ph);
+  const int s = k.stage;
+  const float cst = (s == 2) ? k.c_full : k.c_half;
+  if (s == 0) {
+    st8(Acc + e, f);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sv[i] = __fmaf_rn(cst, f[i], ph[i]);
+  } else if (s < 3) {
+    float ac[8];
+    ld8(Acc + e, ac);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      ac[i] = __fmaf_rn(2.f, f[i], ac[i]);
+      sv[i] = __fmaf_rn(cst, f[i], ph[i]);
+    }
+    st8(Acc + e, ac);
+  } else {
+    float ac[8], pl[8];
+    ld8(Acc + e, ac);
+    ld8(Plo + e, pl);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      ph[i] = rk4_final_f32(ph[i], ac[i], f[i], k.c_sixth, k.c_sixth_lo, pl[i]);
+      sv[i] = ph[i];
+      bad |= !isfinite(ph[i]);
+    }
+    st8(Phi + e, ph);
+    st8(Plo + e, pl);
+  }
+}
+
+__device__ __forceinline__ void epi_bar() { asm volatile("bar.sync 1, %0;" ::"n"(kEpiThreads) : "memory"); }
+
+// The operands and scaling of one tile.
+struct Tile {
+  const uint8_t* A[3];     // A pieces of this tile's 128-row block, chunk 0 (chunk c at + c * kPiece)
+  const uint8_t* B[2];     // B pieces of this tile's 128-column block, chunk 0
+  int c0, n_chunks;        // chunk range [c0, c0 + n_chunks), n_chunks a multiple of kGroup
+  const float* row_inv;    // 128 per-row inverse A scales of the tile (0 on padding rows)
+  float inv_sb;            // inverse B scale
+  uint32_t max_wait;       // bound on every mbarrier poll loop
+};
+
+// TMEM allocation and barrier set-up; every thread of the CTA calls it.
+__device__ __forceinline__ void setup(Smem& S) {
+  const int t = threadIdx.x, warp = t >> 5;
+  if (warp == 0) {
+    tc::tmem_alloc(&S.tmem_base, kTmemCols);
+    tc::tmem_relinquish();
+  }
+  if (t == 32) {
+    for (int s = 0; s < kStages; ++s) {
+      tc::mbar_init(&S.full[s], 1);
+      tc::mbar_init(&S.empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&S.accf[b], 1);
+      tc::mbar_init(&S.acce[b], kEpiThreads);
+    }
+    tc::mbar_init(&S.drain, 1);
+    S.abort = 0;
+    tc::mbar_fence_init();
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+}
+
+// Every thread: waits for the CTA, raises LIME_FLAG_TIMEOUT if a wait
+// expired, releases TMEM.
+__device__ __forceinline__ void teardown(Smem& S, int32_t* status) {
+  tc::tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && S.abort) atomicOr(status, LIME_FLAG_TIMEOUT);
+  if ((threadIdx.x >> 5) == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(S.tmem_base, kTmemCols);
+  }
+}
+
+// The tile's main loop.  Returns true on the 256 epilogue threads, which on
+// return have parked C[r][c] * row_inv[r] * inv_sb at S.tile()[c * kFStride
+// + r] and passed a named barrier together (unless S.abort is set: a wait
+// expired and the tile is not valid); false on the producer and MMA warps.
+__device__ __forceinline__ bool mainloop(Smem& S, const Tile& T) {
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const uint32_t tbase = S.tmem_base;
+  const int KC = T.n_chunks;
+
+  if (warp == 0) {
+    // ---------------- producer
+    if (lane == 0) {
+      int issued = 0;
+      for (int c = 0; c < KC; ++c) {
+        const int s = c % kStages;
+        const uint32_t ph = (uint32_t)(c / kStages) & 1u;
+        if (!tc::mbar_wait_bounded(&S.empty[s], ph ^ 1u, T.max_wait)) { atomicExch(&S.abort, 1); break; }
+        if (*(volatile int*)&S.abort) break;
+        issued = c + 1;
+        tc::mbar_arrive_expect_tx(&S.full[s], 5 * kPiece);
+        const size_t off = (size_t)(T.c0 + c) * kPiece;
+        tc::bulk_g2s(S.stage[s][0], T.A[0] + off, kPiece, &S.full[s]);
+        tc::bulk_g2s(S.stage[s][1], T.A[1] + off, kPiece, &S.full[s]);
+        tc::bulk_g2s(S.stage[s][2], T.A[2] + off, kPiece, &S.full[s]);
+        tc::bulk_g2s(S.stage[s][3], T.B[0] + off, kPiece, &S.full[s]);
+        tc::bulk_g2s(S.stage[s][4], T.B[1] + off, kPiece, &S.full[s]);
+      }
+      // the copies of the last (up to kStages) issued chunks have landed before exit
+      for (int c = issued - 1; c >= 0 && c >= issued - kStages; --c)
+        tc::mbar_wait_bounded(&S.full[c % kStages], (uint32_t)(c / kStages) & 1u, T.max_wait);
+    }
+    return false;
+  }
+  if (warp == 1) {
+    // ---------------- MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t idesc = tc::idesc_f16(kBM, kBN, 0);
+      for (int c = 0; c < KC; ++c) {
+        const int s = c % kStages;
+        const uint32_t ph = (uint32_t)(c / kStages) & 1u;
+        const int p = c / kGroup, b = p & 1;
+        const bool first = (c % kGroup) == 0;
+        const bool last = (c % kGroup) == kGroup - 1;
+        if (!tc::mbar_wait_bounded(&S.full[s], ph, T.max_wait)) { atomicExch(&S.abort, 1); break; }
+        if (first && !tc::mbar_wait_bounded(&S.acce[b], ((uint32_t)(p >> 1) & 1u) ^ 1u, T.max_wait)) {
+          atomicExch(&S.abort, 1);
+          break;
+        }
+        if (*(volatile int*)&S.abort) break;
+        tc::tc_fence_after();
+        const uint32_t d0 = tbase + (uint32_t)(2 * b) * 128u;
+        const uint32_t d1 = d0 + 128u;
+        const uint32_t base = tc::smem_u32(S.stage[s][0]);
+#pragma unroll
+        for (int ks = 0; ks < kCK / 16; ++ks) {
+          const uint32_t ko = (uint32_t)ks * 2u * kLBO;
+          const uint64_t a0 = tc::smem_desc_noswizzle(base + 0 * kPiece + ko, kLBO, kSBO);
+          const uint64_t a1 = tc::smem_desc_noswizzle(base + 1 * kPiece + ko, kLBO, kSBO);
+          const uint64_t a2 = tc::smem_desc_noswizzle(base + 2 * kPiece + ko, kLBO, kSBO);
+          const uint64_t b0 = tc::smem_desc_noswizzle(base + 3 * kPiece + ko, kLBO, kSBO);
+          const uint64_t b1 = tc::smem_desc_noswizzle(base + 4 * kPiece + ko, kLBO, kSBO);
+          const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+          tc::mma_f16_ss(d0, a0, b0, idesc, acc);
+          tc::mma_f16_ss(d1, a1, b0, idesc, acc);
+          tc::mma_f16_ss(d1, a0, b1, idesc, 1u);
+          tc::mma_f16_ss(d1, a1, b1, idesc, 1u);
+          tc::mma_f16_ss(d1, a2, b0, idesc, 1u);
+        }
+        tc::mma_commit(&S.empty[s]);
+        if (last) tc::mma_commit(&S.accf[b]);
+      }
+      // every MMA this thread issued has completed before TMEM is released
+      tc::mma_commit(&S.drain);
+      tc::mbar_wait_bounded(&S.drain, 0u, T.max_wait);
+    }
+    return false;
+  }
+
+  // ---------------- epilogue: 8 warps, TMEM lane quadrant warp & 3, column half
+  const int lq = warp & 3;
+  const int h = (warp - 2) >> 2;
+  const int r = lq * 32 + lane;
+  const uint32_t lane_addr = tbase + ((uint32_t)(lq * 32) << 16);
+  // hi words in registers, lo words in shared memory (each thread owns its
+  // 64 entries; lanes hit consecutive words)
+  float hi[64];
+  float* lo = S.lo + (64 * h) * kBM + r;
+#pragma unroll
+  for (int c = 0; c < 64; ++c) { hi[c] = 0.f; lo[c * kBM] = 0.f; }
+  const int n_groups = KC / kGroup;
+  bool ok = true;
+  for (int p = 0; p < n_groups; ++p) {
+    const int b = p & 1;
+    if (!tc::mbar_wait_bounded(&S.accf[b], (uint32_t)(p >> 1) & 1u, T.max_wait)) {
+      atomicExch(&S.abort, 1);
+      ok = false;
+      break;
+    }
+    tc::tc_fence_after();
+    const uint32_t d0 = lane_addr + (uint32_t)(2 * b) * 128u + 64u * h;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      // (one load and wait per accumulator measured faster than both loads
+      // under one wait)
+      float v[16], er[16];
+      tc::tmem_ld16(d0 + 16 * q, v);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        // exact D0 into the two-sum
+        const float x = v[e];
+        const float sm = __fadd_rn(hi[16 * q + e], x);
+        const float bv = __fsub_rn(sm, hi[16 * q + e]);
+        er[e] = __fadd_rn(__fsub_rn(hi[16 * q + e], __fsub_rn(sm, bv)), __fsub_rn(x, bv));
+        hi[16 * q + e] = sm;
+      }
+      tc::tmem_ld16(d0 + 128u + 16 * q, v);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        float* l = lo + (16 * q + e) * kBM;
+        *l = __fadd_rn(*l, __fadd_rn(er[e], v[e]));
+      }
+    }
+    tc::tc_fence_before();
+    tc::mbar_arrive(&S.acce[b]);
+  }
+  // park the tile in the ring: every MMA has completed once the last
+  // accumulator group was seen, so the tensor core reads no operand
+  const float rs = __fmul_rn(T.row_inv[r], T.inv_sb);
+  float* ft = S.tile();
+  if (ok) {
+#pragma unroll
+    for (int c = 0; c < 64; ++c) ft[(64 * h + c) * kFStride + r] = __fmul_rn(__fadd_rn(hi[c], lo[c * kBM]), rs);
+  }
+  epi_bar();
+  return true;
+}
+
+// ---------------------------------------------------------------- operand conversion
+// A pieces of one row (row = blockIdx.x) of the real block row [Mr | Mi] of
+// a complex matrix M (rows x cols, row stride ld; element (row, kk) read by
+// elem).  The row is scaled by the power of two that brings its largest
+// component into [2^12, 2^13) and split as A0 = 64 k (|k| <= 127) + fp16
+// residuals A1, A2; row_inv gets the inverse scale (0 for padding rows and
+// all-zero rows).  Columns kk >= cols are zero; Kp is the padded column
+// count (the imaginary block starts at Kp), KC the chunks per row tile.
+template <class Elem>
+__device__ __forceinline__ void convert_row(const Elem& elem, int row, bool valid, int cols, int Kp, int KC,
+                                            uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
+  __shared__ double red[32];
+  double mx = 0.0;
+  if (valid)
+    for (int k = threadIdx.x; k < cols; k += blockDim.x) {
+      const double2 z = elem(k);
+      mx = fmax(mx, fmax(fabs(z.x), fabs(z.y)));
+    }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[w]);
+    red[0] = m;
+  }
+  __syncthreads();
+  mx = red[0];
+  int sh = 0;
+  bool live = valid && mx > 0.0 && isfinite(mx);
+  if (live) {
+    sh = 12 - ilogb(mx);                 // mx * 2^sh in [2^12, 2^13)
+    if (sh > 140 || sh < -140) live = false;
+  }
+  if (threadIdx.x == 0) row_inv[row] = live ? ldexpf(1.f, -sh) : 0.f;
+  for (int k = threadIdx.x; k < 2 * Kp; k += blockDim.x) {
+    double x = 0.0;
+    if (live) {
+      const int kk = k < Kp ? k : k - Kp;
+      if (kk < cols) {
+        const double2 z = elem(kk);
+        x = ldexp(k < Kp ? z.x : z.y, sh);
+      }
+    }
+    const double kq = fmin(fmax(rint(x * (1.0 / 64.0)), -kA0Max), kA0Max);
+    const double v0 = kq * 64.0;
+    const double r1 = x - v0;
+    const __half h1 = __double2half(r1);
+    const __half h2 = __double2half(r1 - (double)__half2float(h1));
+    const size_t off = piece_off(KC, row, k);
+    *reinterpret_cast<__half*>(A0 + off) = __double2half(v0);
+    *reinterpret_cast<__half*>(A1 + off) = h1;
+    *reinterpret_cast<__half*>(A2 + off) = h2;
+  }
+}
+
+}  // namespace sg
+}  // namespace lime

@@ -301,6 +301,75 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
     return obs_out[:, :, :n_obs], None, status
 
 
+def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
+                obs_every: int, param_batch: int, events=None, max_retries: int = 3):
+    """Any generator on the tensor cores (``lime_lindblad_rk4_stream``):
+    streaming split-precision GEMMs for Heff rho and sum_k L_k rho L_k^dag.
+    State scale: max |rho0| * 1.25 <= 2^13; L_k rho scale from the largest
+    absolute row sum of the collapse operators; a run whose values leave the
+    fixed-point range raises LIME_FLAG_RANGE and is repeated with both
+    scales lowered 4x."""
+    lib = nat.require_device()
+    B, n = rho.shape[0], gen.n
+    dev = rho.device
+    K = gen.k_dense
+    E = None
+    n_obs = 0
+    if e_ops:
+        Es = [as_device(e, dev) for e in e_ops]
+        if any(e.dim() == 3 for e in Es):
+            E = torch.stack([e.expand(gen.P, n, n) if e.dim() == 2 else e for e in Es], 1).contiguous()
+        else:
+            E = torch.stack(Es, 0).unsqueeze(0).contiguous()
+        n_obs = E.shape[1]
+    n_slots = n_steps // obs_every
+    obs_out = torch.zeros((B, max(n_slots, 1), max(n_obs, 1)), dtype=CDT, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    pmax = float(torch.view_as_real(rho).abs().max().item()) if rho.numel() else 0.0
+    lrow = 0.0
+    if K:
+        lrow = float(gen.l_dense.abs().sum(-1).max().item())
+    sb = _pow2_exponent(8192.0 / 1.25, pmax)
+    sy = _pow2_exponent(8192.0 / 1.25, lrow * pmax) if K else 0
+    heff_shared = gen.heff.shape[0] == 1
+    l_shared = gen.l_dense is None or gen.l_dense.shape[0] == 1
+    G = 1 if (heff_shared and l_shared) else param_batch
+    wsb = lib.lime_lindblad_stream_workspace(n, B, G, K)
+    ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
+    aligned = (ws.data_ptr() + 1023) // 1024 * 1024
+    start = rho.contiguous()
+    for attempt in range(max_retries + 1):
+        work = start.clone()
+        status.zero_()
+        d = nat.LindbladStreamDesc()
+        d.n, d.batch, d.param_batch, d.n_ops = n, B, param_batch, K
+        d.n_steps, d.n_obs, d.obs_every = n_steps, n_obs, obs_every
+        d.scale_b_log2, d.scale_y_log2 = max(-60, min(60, sb)), max(-60, min(60, sy))
+        d.dt = float(dt)
+        d.rho = work.data_ptr()
+        d.heff, d.heff_stride = gen.heff.data_ptr(), (0 if heff_shared else n * n)
+        if gen.m is not None:
+            d.m, d.m_stride = gen.m.data_ptr(), (0 if gen.m.shape[0] == 1 else n * n)
+        if K:
+            d.l_ops, d.l_stride = gen.l_dense.data_ptr(), (0 if l_shared else K * n * n)
+        if E is not None:
+            d.obs_ops, d.obs_stride = E.data_ptr(), (0 if E.shape[0] == 1 else n_obs * n * n)
+            d.obs_out = obs_out.data_ptr()
+        d.workspace, d.workspace_bytes = aligned, wsb
+        d.status = status.data_ptr()
+        if events is not None:
+            events[0].record()
+        nat.check(lib.lime_lindblad_rk4_stream(d, _stream_ptr()), 'lime_lindblad_rk4_stream')
+        if events is not None:
+            events[1].record()
+        if attempt < max_retries and int(status.item()) & nat.LIME_FLAG_RANGE:
+            sb -= 2
+            sy -= 2
+            continue
+        break
+    return obs_out[:, :n_slots, :n_obs], None, status, work
+
+
 def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
             obs_every: int = 1, events=None, drive=None):
@@ -341,9 +410,13 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
         if states_every:
             raise ValueError('precision="split" keeps the state on chip; states_every is not '
                              'supported (use precision="fp64" for rholist output)')
-        tol = 1e-5 if trace_tol is None else trace_tol
-        o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
-                                  param_batch=B, events=events)
+        if split_supported(gen) is None:
+            tol = 1e-5 if trace_tol is None else trace_tol
+            o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
+                                      param_batch=B, events=events)
+        else:
+            o, s, status, work = _run_stream(gen, work, dt, n_steps, e_ops, obs_every,
+                                             param_batch=B, events=events)
     else:
         raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
 
@@ -401,9 +474,9 @@ def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None
     Instances with equal dimension and operator counts are stacked into one
     batched launch; the launches of different dimensions run concurrently on
     separate CUDA streams and the status words are checked once all are
-    enqueued.  ``precision``: 'fp64', 'split' (every group must be
-    tensor-core capable) or 'auto' (split where ``split_supported``, FP64
-    elsewhere).  Returns three lists in input order: observables
+    enqueued.  ``precision``: 'fp64' or 'split' (the batched tensor-core
+    kernel where it applies, the streaming tensor-core GEMMs elsewhere).
+    Returns three lists in input order: observables
     (n_steps // obs_every, n_obs), states or None, final rho.
     """
     B = len(H_list)
@@ -432,13 +505,10 @@ def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None
             H = torch.stack([as_device(H_list[i], device) for i in idx])
             ops = [torch.stack([as_device(c_ops_list[i][k], device) for i in idx]) for k in range(K)]
             gen = LindbladGenerator.build(H, ops, device=device)
-            prec = precision
-            if precision == 'auto':
-                prec = 'split' if split_supported(gen) is None else 'fp64'
             rho = torch.stack([as_device(rho0_list[i], device) for i in idx])
             E = [torch.stack([as_device(e_ops_list[i][o], device) for i in idx])
                  for o in range(len(e_ops_list[idx[0]]))]
-            fin = _launch(gen, rho, dt, n_steps, E, states_every=states_every, precision=prec,
+            fin = _launch(gen, rho, dt, n_steps, E, states_every=states_every, precision=precision,
                           trace_tol=trace_tol, obs_every=obs_every)
         pending.append((idx, st, fin))
     obs, states, rhos = [None] * B, [None] * B, [None] * B

@@ -71,6 +71,7 @@ def _c_layout(struct_name, fields):
     ('LimeRedfieldBuildDesc', 'RedfieldBuildDesc'),
     ('LimeRedfieldRK4Desc', 'RedfieldRK4Desc'),
     ('LimeRedfieldSplitDesc', 'RedfieldSplitDesc'),
+    ('LimeLindbladStreamDesc', 'LindbladStreamDesc'),
 ])
 def test_descriptor_layout_matches_c(tmp_path, cname, pyname):
     from lime_gb300 import _native

@@ -99,18 +99,6 @@ def test_public_api_split_precision():
     assert np.max(np.abs(rsp.observables - r64.observables)) < POP_TOL
 
 
-def test_unsupported_generators_raise():
-    from lime_gb300 import engine
-    rng = np.random.default_rng(3)
-    H, c_ops = chains.uneven_chain(8, rng)
-    gen = engine.LindbladGenerator.build(H, c_ops)
-    with pytest.raises(ValueError, match='dense'):
-        engine.propagate(gen, chains.ground_dm(8), 0.05, 10, precision='split')
-    big = engine.LindbladGenerator.build(np.eye(80), chains.dephasing_ops(80, 0.01))
-    with pytest.raises(ValueError, match='dimension'):
-        engine.propagate(big, chains.ground_dm(80), 0.05, 10, precision='split')
-
-
 def test_split_nonfinite_flag():
     from lime_gb300 import _native, engine
     w, c_ops = _ensemble(8, 2, 10)

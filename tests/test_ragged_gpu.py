@@ -62,9 +62,10 @@ def test_uneven_batch_from_workload_generator():
         assert rel(res[i].observables, ro) < RTOL
 
 
-def test_uneven_batch_auto_precision():
-    """'auto': dephasing groups with n <= 64 take the tensor-core path, the
-    rest FP64; both agree with FP64 to the split path's bar."""
+def test_uneven_batch_split_precision():
+    """precision='split' on every size group: the dephasing groups with
+    n <= 64 take the batched kernel, the 70-dim one the streaming GEMMs;
+    all agree with FP64 to the split path's bar."""
     from lime_gb300 import engine
     rng = np.random.default_rng(5)
     sizes = [16, 40, 16, 70]
@@ -77,14 +78,10 @@ def test_uneven_batch_auto_precision():
         R.append(chains.ground_dm(n))
         E.append(chains.population_ops(n)[:4])
     o64, _, r64 = engine.propagate_ragged(H, R, 0.05, 200, C, E)
-    oau, _, rau = engine.propagate_ragged(H, R, 0.05, 200, C, E, precision='auto')
+    osp, _, rsp = engine.propagate_ragged(H, R, 0.05, 200, C, E, precision='split')
     for i in range(len(sizes)):
-        assert np.max(np.abs((oau[i] - o64[i]).cpu().numpy())) < 1e-6
-        assert np.max(np.abs((rau[i] - r64[i]).cpu().numpy())) < 1e-6
-    # the 70-dim instance ran FP64 (exact agreement), the others split
-    assert np.max(np.abs((oau[3] - o64[3]).cpu().numpy())) < 1e-12
-    with pytest.raises(ValueError):
-        engine.propagate_ragged(H, R, 0.05, 10, C, E, precision='split')
+        assert np.max(np.abs((osp[i] - o64[i]).cpu().numpy())) < 1e-6
+        assert np.max(np.abs((rsp[i] - r64[i]).cpu().numpy())) < 1e-6
 
 
 def test_uneven_batch_argument_errors():
