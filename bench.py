@@ -57,6 +57,8 @@ def parse():
     p.add_argument('--no-ragged', action='store_true')
     p.add_argument('--redfield-only', action='store_true',
                    help='run only the dense Redfield leg and print its JSON')
+    p.add_argument('--ragged-only', action='store_true',
+                   help='run only the uneven-batch leg and print its JSON')
     p.add_argument('--redfield-n', type=int, default=96)
     p.add_argument('--redfield-rhs', type=int, default=512)
     return p.parse_args()
@@ -174,6 +176,10 @@ def gpu_arm(args, rank, world, local):
     lbuild.build()
     nat.require_device()
 
+    if args.ragged_only:
+        if rank == 0:
+            print(json.dumps(ragged_leg(torch, dev)))
+        return
     if args.redfield_only:
         if rank == 0:
             print(json.dumps(redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n,
@@ -429,30 +435,57 @@ def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k
                                  'observable launch'}}
 
 
-def ragged_leg(torch, dev, batch=1024, steps=2):
+def ragged_leg(torch, dev, batch=1024, steps_split=40, steps_fp64=2, err_steps=200):
     """Uneven batch: 1024 chains with N uniform over {8..256}, three dense
-    complex collapse operators each (2000-step workload; a sample of steps
-    is timed), through the public uneven-batch API: every size group is one
-    batched FP64 launch, the groups run concurrently on their own streams.
-    Dense collapse operators are outside the tensor-core kernel, so this is
-    the FP64 rate."""
+    complex collapse operators each (2000-step workload; samples of steps
+    are timed), through the public uneven-batch API: every size group is one
+    batched launch sequence, the groups run concurrently on their own
+    streams.  Split precision (streaming tensor-core GEMMs) against the FP64
+    path: rates on the whole batch, and the split error on populations over
+    err_steps steps on two chains of every size up to 128."""
+    import numpy as np
     from lime_gb300 import chains, engine
-    w = chains.uneven_batch(batch=batch, n_steps=steps)
+    w = chains.uneven_batch(batch=batch, n_steps=steps_split)
     ns = w['ns']
     E = [[chains.population_ops(int(n))[0]] for n in ns]
-    engine.propagate_ragged(w['H'], w['rho0'], w['dt'], 1, w['c_ops'], E)   # warm
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    engine.propagate_ragged(w['H'], w['rho0'], w['dt'], steps, w['c_ops'], E)
-    torch.cuda.synchronize()
-    t = time.perf_counter() - t0
-    flop = float(sum(256.0 * int(n) ** 3 for n in ns)) * steps   # 64 (1 + K) N^3, K = 3
+
+    def run(steps, precision, idx=None):
+        sel = range(len(ns)) if idx is None else idx
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = engine.propagate_ragged([w['H'][i] for i in sel], [w['rho0'][i] for i in sel], w['dt'],
+                                      steps, [w['c_ops'][i] for i in sel], [E[i] for i in sel],
+                                      precision=precision)
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    run(1, 'split')   # warm
+    run(1, 'fp64')
+    _, ts1 = run(steps_split // 2, 'split')
+    _, ts = run(steps_split, 'split')
+    _, tf = run(steps_fp64, 'fp64')
+    per_step = (ts - ts1) / (steps_split - steps_split // 2)
+    sub = [i for s in sorted(set(int(n) for n in ns)) if s <= 128 for i in np.flatnonzero(ns == s)[:2]]
+    (o64, _, _), _ = run(err_steps, 'fp64', sub)
+    (osp, _, _), _ = run(err_steps, 'split', sub)
+    err = max(float((a - b).abs().max().item()) for a, b in zip(osp, o64))
+    flop = float(sum(256.0 * int(n) ** 3 for n in ns))   # 64 (1 + K) N^3 per instance-step, K = 3
+    split_rate = len(ns) / per_step
+    fp64_rate = len(ns) * steps_fp64 / tf
     return {'workload': 'uneven batch: %d chains, N uniform over {8,16,32,64,128,256}, '
                         'tridiagonal + 0.01 GOE, 3 dense complex collapse operators' % len(ns),
-            'path': 'fp64 (one batched launch per size, groups on concurrent streams)',
-            'unit': 'instance-steps/s', 'value': len(ns) * steps / t, 'steps': steps,
-            'wall_s_incl_setup': t, 'algorithmic_tflops': flop / t / 1e12,
-            'note': 'wall time of the public call, including generator preparation'}
+            'unit': 'instance-steps/s',
+            'split': {'value': split_rate, 'ms_per_step': per_step * 1e3,
+                      'sample': 'difference of %d- and %d-step calls' % (steps_split // 2, steps_split),
+                      'wall_s_incl_setup': ts, 'steps_in_wall': steps_split,
+                      'algorithmic_tflops': flop / per_step / 1e12,
+                      'path': 'streaming tcgen05 GEMMs (Heff rho, L rho L^dag), one launch '
+                              'sequence per size, groups on concurrent streams'},
+            'fp64_gpu': {'value': fp64_rate, 'steps': steps_fp64, 'wall_s': tf},
+            'speedup_vs_fp64_gpu': split_rate / fp64_rate,
+            'split_max_population_error': err,
+            'error_sample': '%d chains (two of each N <= 128), %d steps' % (len(sub), err_steps),
+            'note': 'fp64 rate: wall time of the public call including set-up'}
 
 
 def e2e_leg(wl, K, path, dev):
