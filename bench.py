@@ -59,6 +59,12 @@ def parse():
                    help='run only the dense Redfield leg and print its JSON')
     p.add_argument('--ragged-only', action='store_true',
                    help='run only the uneven-batch leg and print its JSON')
+    p.add_argument('--adjoint-only', action='store_true',
+                   help='run only the adjoint/forward leg and print its JSON')
+    p.add_argument('--adjoint-batch', type=int, default=256)
+    p.add_argument('--ragged-batch', type=int, default=1024)
+    p.add_argument('--ragged-sizes', default='8,16,32,64,128,256',
+                   help='comma-separated chain sizes of the uneven batch')
     p.add_argument('--redfield-n', type=int, default=96)
     p.add_argument('--redfield-rhs', type=int, default=512)
     return p.parse_args()
@@ -176,9 +182,14 @@ def gpu_arm(args, rank, world, local):
     lbuild.build()
     nat.require_device()
 
+    if args.adjoint_only:
+        if rank == 0:
+            print(json.dumps(adjoint_leg(torch, dev, batch=args.adjoint_batch)))
+        return
     if args.ragged_only:
         if rank == 0:
-            print(json.dumps(ragged_leg(torch, dev)))
+            print(json.dumps(ragged_leg(torch, dev, batch=args.ragged_batch,
+                                        sizes=tuple(int(x) for x in args.ragged_sizes.split(',')))))
         return
     if args.redfield_only:
         if rank == 0:
@@ -238,13 +249,14 @@ def gpu_arm(args, rank, world, local):
         e2e = e2e_leg(wl, K, path, dev)
     adj = None
     if not args.no_adjoint and rank == 0:
-        adj = adjoint_leg(torch, dev)
+        adj = adjoint_leg(torch, dev, batch=args.adjoint_batch)
     red = None
     if not args.no_redfield and rank == 0:
         red = redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n, n_rhs=args.redfield_rhs)
     rag = None
     if not args.no_ragged and rank == 0:
-        rag = ragged_leg(torch, dev)
+        rag = ragged_leg(torch, dev, batch=args.ragged_batch,
+                         sizes=tuple(int(x) for x in args.ragged_sizes.split(',')))
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -435,7 +447,8 @@ def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k
                                  'observable launch'}}
 
 
-def ragged_leg(torch, dev, batch=1024, steps_split=40, steps_fp64=2, err_steps=200):
+def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_split=40, steps_fp64=2,
+               err_steps=200):
     """Uneven batch: 1024 chains with N uniform over {8..256}, three dense
     complex collapse operators each (2000-step workload; samples of steps
     are timed), through the public uneven-batch API: every size group is one
@@ -445,7 +458,7 @@ def ragged_leg(torch, dev, batch=1024, steps_split=40, steps_fp64=2, err_steps=2
     err_steps steps on two chains of every size up to 128."""
     import numpy as np
     from lime_gb300 import chains, engine
-    w = chains.uneven_batch(batch=batch, n_steps=steps_split)
+    w = chains.uneven_batch(batch=batch, sizes=sizes, n_steps=steps_split)
     ns = w['ns']
     E = [[chains.population_ops(int(n))[0]] for n in ns]
 
@@ -465,15 +478,16 @@ def ragged_leg(torch, dev, batch=1024, steps_split=40, steps_fp64=2, err_steps=2
     _, ts = run(steps_split, 'split')
     _, tf = run(steps_fp64, 'fp64')
     per_step = (ts - ts1) / (steps_split - steps_split // 2)
-    sub = [i for s in sorted(set(int(n) for n in ns)) if s <= 128 for i in np.flatnonzero(ns == s)[:2]]
+    small = [s for s in sorted(set(int(n) for n in ns)) if s <= 128] or [int(min(ns))]
+    sub = [int(i) for s in small for i in np.flatnonzero(ns == s)[:2]]
     (o64, _, _), _ = run(err_steps, 'fp64', sub)
     (osp, _, _), _ = run(err_steps, 'split', sub)
     err = max(float((a - b).abs().max().item()) for a, b in zip(osp, o64))
     flop = float(sum(256.0 * int(n) ** 3 for n in ns))   # 64 (1 + K) N^3 per instance-step, K = 3
     split_rate = len(ns) / per_step
     fp64_rate = len(ns) * steps_fp64 / tf
-    return {'workload': 'uneven batch: %d chains, N uniform over {8,16,32,64,128,256}, '
-                        'tridiagonal + 0.01 GOE, 3 dense complex collapse operators' % len(ns),
+    return {'workload': 'uneven batch: %d chains, N uniform over {%s}, tridiagonal + 0.01 GOE, '
+                        '3 dense complex collapse operators' % (len(ns), ','.join(str(x) for x in sizes)),
             'unit': 'instance-steps/s',
             'split': {'value': split_rate, 'ms_per_step': per_step * 1e3,
                       'sample': 'difference of %d- and %d-step calls' % (steps_split // 2, steps_split),
@@ -484,7 +498,8 @@ def ragged_leg(torch, dev, batch=1024, steps_split=40, steps_fp64=2, err_steps=2
             'fp64_gpu': {'value': fp64_rate, 'steps': steps_fp64, 'wall_s': tf},
             'speedup_vs_fp64_gpu': split_rate / fp64_rate,
             'split_max_population_error': err,
-            'error_sample': '%d chains (two of each N <= 128), %d steps' % (len(sub), err_steps),
+            'error_sample': '%d chains (two of each N <= 128, else of the smallest N), %d steps'
+                            % (len(sub), err_steps),
             'note': 'fp64 rate: wall time of the public call including set-up'}
 
 
