@@ -330,15 +330,19 @@ int lime_lindblad_rk4_f64_noalloc(const LimeLindbladDesc* d, void* stream);
 /* ------------------------------------------------------------------ */
 
 /* RK4 propagation of B Hermitian density matrices (n <= 64) on the tcgen05
- * tensor cores: each stage's Heff * rho is an fp16 hi/lo split product
- * (three MMAs, fp32 accumulation) of power-of-two pre-scaled operands; the
+ * tensor cores: each stage's Heff * rho is a split-precision product (A:
+ * per-row 7-bit fixed point + two fp16 residuals, B: per-row 10-bit fixed
+ * point + fp16 residual, exact dominant product) of power-of-two pre-scaled
+ * operands; the
  * state is fp32 with an fp32 compensation term; observables, traces and the
  * final state are produced in FP64.  Replaces the same loops as
  * lime_lindblad_rk4_f64 (lime/oqs.py:1674-1682, 777-787) for generators
  * whose collapse operators are site-diagonal projectors or any diagonal
  * operators with diagonal M (pure dephasing): m_diag[p][i] = M_ii.
  *   scale_a_log2  A = Heff * 2^scale_a_log2 (choose max|A| ~ 2^12)
- *   scale_b_log2  B = rho  * 2^scale_b_log2 (choose a bound of |rho_ij| ~ 2^13)
+ *   scale_b_log2  B = rho  * 2^scale_b_log2 (choose a bound of |rho_ij| ~ 2^13;
+ *                 each B row then gets its own fixed-point quantum from the
+ *                 previous stage's row bound)
  *   obs_mode      0 none; 1 populations: obs k = rho_kk (n_obs <= n);
  *                 2 dense: obs_ops [P|1][n_obs][n][n], Tr(E rho)
  *   obs_out       [B][n_steps / obs_every][n_obs] complex128

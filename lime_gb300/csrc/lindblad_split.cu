@@ -27,7 +27,8 @@
 // the same TMEM columns; their truncation bias is ~2^-27 of X.  The two
 // partial results are summed in fp32 (round to nearest) by the epilogue.
 //
-// Epilogue (4 warps; thread t owns TMEM lane t, i.e. row t of [Xr; Xi]):
+// Epilogue (8 warps; thread (r, h) owns TMEM lane r, i.e. row r of [Xr; Xi],
+// columns [32 h, 32 h + 32)):
 // threads 0..63 form Im f[i][:] = Xr[j][i] - Xr[i][j], threads 64..127 form
 // Re f[i][:] = Xi[i][j] + Xi[j][i] (the X^dag half comes through a shared
 // transpose buffer), add the dephasing jump term m_i rho_ii, and fuse the RK4

@@ -265,6 +265,10 @@ def _split_obs(e_ops, n, P, device):
 def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
                obs_every: int, trace_tol: float, param_batch: int, events=None,
                ctas_per_sm: int = 0):
+    """The batched tensor-core kernel (n <= 64, diagonal collapse operators).
+    State scale: sqrt(n) ||rho(0)||_F (a bound of |rho_ij(t)|: the trace
+    norm contracts) at 2^13; the kernel picks each B row's fixed-point
+    quantum from the previous stage's row bound."""
     lib = nat.require_device()
     why = split_supported(gen)
     if why is not None:
@@ -278,11 +282,12 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
         m_diag = torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous()
     amax = float(gen.heff.abs().max().item())
     rbound = float(torch.linalg.matrix_norm(rho).max().item()) * (n ** 0.5)
+    sb = _pow2_exponent(8192.0, rbound)
     d = nat.SplitDesc()
     d.n, d.batch, d.param_batch, d.n_steps = n, B, param_batch, n_steps
     d.obs_mode, d.n_obs, d.obs_every = mode, n_obs, obs_every
     d.scale_a_log2 = _pow2_exponent(4096.0, amax)
-    d.scale_b_log2 = _pow2_exponent(8192.0, rbound)
+    d.scale_b_log2 = max(-60, min(60, sb))
     d.ctas_per_sm = ctas_per_sm
     d.dt, d.trace_tol = float(dt), float(trace_tol)
     d.rho = rho.data_ptr()
