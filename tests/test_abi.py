@@ -53,6 +53,45 @@ def test_null_descriptor_rejected(lib):
     # argument validation happens before any CUDA call
     assert lib.lime_lindblad_rk4_f64(None, None) == -1
     assert lib.lime_lindblad_prepare_f64(None, None) == -1
+    assert lib.lime_lindblad_rk4_split(None, None) == -1
+    assert lib.lime_lindblad_rk4_stream(None, None) == -1
+    assert lib.lime_redfield_rk4_split(None, None) == -1
+    assert lib.lime_redfield_rk4_f64(None, None) == -1
+    assert lib.lime_lindblad_adjoint_f64(None, None) == -1
+
+
+def test_stream_descriptor_validation(lib):
+    """Host-side checks of the streaming entry point (no CUDA call is made
+    before they pass): sizes, missing pointers, scales, workspace, alignment."""
+    from lime_gb300 import _native
+    d = _native.LindbladStreamDesc()
+    d.n, d.batch, d.n_ops, d.n_steps, d.dt = 8, 2, 1, 3, 0.05
+    assert lib.lime_lindblad_rk4_stream(ctypes.byref(d), None) == -1      # no pointers
+    d.rho, d.heff, d.status, d.workspace = 0x1000, 0x2000, 0x3000, 0x410
+    assert lib.lime_lindblad_rk4_stream(ctypes.byref(d), None) == -1      # l_ops missing
+    d.l_ops = 0x5000
+    d.scale_b_log2 = 99
+    assert lib.lime_lindblad_rk4_stream(ctypes.byref(d), None) == -1      # scale out of range
+    d.scale_b_log2 = 0
+    d.workspace_bytes = 16
+    assert lib.lime_lindblad_rk4_stream(ctypes.byref(d), None) == -5      # workspace too small
+    d.workspace_bytes = lib.lime_lindblad_stream_workspace(8, 2, 2, 1)
+    assert lib.lime_lindblad_rk4_stream(ctypes.byref(d), None) == -1      # workspace not 1024-aligned
+    d.n = 5000
+    assert lib.lime_lindblad_rk4_stream(ctypes.byref(d), None) == -2      # unsupported size
+
+
+def test_stream_and_redfield_workspace_queries(lib):
+    # n padded to 64: A1 pieces 3 x MT1 x KC1 x 16 KB etc.; monotone in every size
+    w = lib.lime_lindblad_stream_workspace
+    assert w(0, 1, 1, 0) == 0 and w(8, 0, 1, 0) == 0
+    assert w(8, 1, 1, 3) == w(64, 1, 1, 3)          # same padded dimension
+    assert w(65, 1, 1, 3) > w(64, 1, 1, 3)
+    assert w(64, 4, 4, 3) > w(64, 4, 1, 3) > w(64, 2, 1, 3)
+    r = lib.lime_redfield_split_workspace
+    assert r(0, 4, 0) == 0
+    assert r(8, 64, 0) == r(8, 1, 0)                # right-hand sides padded to 64
+    assert r(8, 64, 200) > r(8, 64, 100) > r(8, 64, 0)
 
 
 def _c_layout(struct_name, fields):
