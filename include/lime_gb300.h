@@ -300,6 +300,49 @@ typedef struct {
 size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops);
 int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream);
 
+/* Discrete adjoint of the RK4 steps of lime_lindblad_rk4_stream for the
+ * chain model (site energies on the diagonal, nearest-neighbour bonds, site
+ * dephasing; no dense collapse operators): the same backward recursion and
+ * gradient sums as lime_lindblad_adjoint_f64, over all segments in one
+ * call, on the tensor cores.  Per segment (from the last): recompute the
+ * forward steps from the checkpoint, storing every stage input, then walk
+ * the steps backwards applying the adjoint generator (G = -Heff^dag, conj M)
+ * through the same streaming GEMM.
+ *   ckpt      [n_seg][B][n][n] complex128: the state at steps 0, seg, 2 seg, ...
+ *   lam       [B][n][n] complex128 out (adjoint state at step 0) or NULL
+ *   heff, heff_adj = -Heff^dag  [P|1][n][n]; m, m_adj = conj(M) or both NULL
+ *   obs_ops   [P|1][n_obs][n][n]; obs_grad [B][n_steps/obs_every][n_obs]
+ *             complex128 = dL/d conj(obs) (torch's convention)
+ *   grad_diag [B][n], grad_bond [B][max(n-1,1)], grad_gamma [B][n] (added to)
+ *   scale_b_log2  power-of-two scale of rho (max |rho| 2^s <= 2^13); the
+ *             adjoint stage inputs are scaled per step from max |lam| on the
+ *             device (LIME_FLAG_RANGE if a value leaves the range)
+ *   scale_l_log2  reserved (0)
+ *   workspace lime_lindblad_adjoint_stream_workspace(n, batch, G, seg_steps),
+ *             1024-byte aligned; G = 1 when heff and heff_adj are shared
+ */
+typedef struct {
+  int32_t n, batch, param_batch, n_steps, seg_steps, n_obs, obs_every;
+  int32_t scale_b_log2, scale_l_log2;
+  double dt;
+  const double* ckpt;
+  double* lam;
+  const double* heff;      int64_t heff_stride;
+  const double* heff_adj;  int64_t heff_adj_stride;
+  const double* m;
+  const double* m_adj;     int64_t m_stride;
+  const double* obs_ops;   int64_t obs_stride;
+  const double* obs_grad;
+  double* grad_diag;
+  double* grad_bond;
+  double* grad_gamma;
+  void* workspace;         size_t workspace_bytes;
+  int32_t* status;
+} LimeLindbladAdjointStreamDesc;
+
+size_t lime_lindblad_adjoint_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t seg_steps);
+int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc* d, void* stream);
+
 /* Same propagation as lime_lindblad_rk4_f64 for callers that cannot allocate
  * device memory: a host framework whose pool owns the GPU, a latency-critical
  * loop where cudaMalloc/cudaFree would synchronise the device, or a process

@@ -147,6 +147,22 @@ class LindbladStreamDesc(ctypes.Structure):
                 ('status', c_void_p)]
 
 
+class AdjointStreamDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('batch', c_int32), ('param_batch', c_int32), ('n_steps', c_int32),
+                ('seg_steps', c_int32), ('n_obs', c_int32), ('obs_every', c_int32),
+                ('scale_b_log2', c_int32), ('scale_l_log2', c_int32),
+                ('dt', c_double),
+                ('ckpt', c_void_p), ('lam', c_void_p),
+                ('heff', c_void_p), ('heff_stride', c_int64),
+                ('heff_adj', c_void_p), ('heff_adj_stride', c_int64),
+                ('m', c_void_p), ('m_adj', c_void_p), ('m_stride', c_int64),
+                ('obs_ops', c_void_p), ('obs_stride', c_int64),
+                ('obs_grad', c_void_p),
+                ('grad_diag', c_void_p), ('grad_bond', c_void_p), ('grad_gamma', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t),
+                ('status', c_void_p)]
+
+
 # (name, restype, argtypes) of every exported symbol; tests check the header
 # declares exactly these.
 SIGNATURES = [
@@ -163,6 +179,8 @@ SIGNATURES = [
     ('lime_redfield_rk4_split', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_lindblad_stream_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_stream', c_int32, [ctypes.POINTER(LindbladStreamDesc), c_void_p]),
+    ('lime_lindblad_adjoint_stream_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
+    ('lime_lindblad_adjoint_stream', c_int32, [ctypes.POINTER(AdjointStreamDesc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),

@@ -17,8 +17,16 @@ Non-Hermitian starting states (the dipole correlation <mu(t) mu(0)> starts
 from mu|g><g|) run as their two Hermitian parts rho = A + iB; for complex
 observables torch's convention dL = Re sum conj(grad) d(obs) makes the
 source of the B chain ``-i grad``.
+
+``precision='split'`` runs the same computation on the tensor cores: the
+forward pass segment by segment through the split-precision propagators
+(keeping the checkpoints), the backward pass through
+``lime_lindblad_adjoint_stream`` (the same discrete adjoint on the streaming
+split-precision GEMMs).
 """
 from __future__ import annotations
+
+import math
 
 import torch
 
@@ -50,9 +58,87 @@ def dephasing_diagonals(gamma: torch.Tensor, N: int, site0: int) -> torch.Tensor
     return l
 
 
+def _forward_split(gen, work, dt, n_steps, E, obs_every, B, K):
+    """Split-precision forward in segments of K steps: observables and the
+    states at steps 0, K, 2K, ... (the checkpoints, complex128)."""
+    ckpts, parts = [], []
+    done = 0
+    while done < n_steps:
+        seg = min(K, n_steps - done)
+        ckpts.append(work.clone())
+        if engine.split_supported(gen) is None:
+            o, _, status = engine._run_split(gen, work, dt, seg, E, obs_every, 1e-5, param_batch=B)
+        else:
+            o, _, status, work = engine._run_stream(gen, work, dt, seg, E, obs_every, param_batch=B)
+        flags = int(status.item())
+        if flags:
+            raise nat.KernelFlagError(flags, 'chain_observables forward (split)')
+        parts.append(o)
+        done += seg
+    return torch.cat(parts, 1), torch.stack(ckpts, 0).contiguous()
+
+
+def _pow2_scale(bound: float) -> int:
+    """Largest power-of-two exponent s with 1.25 * bound * 2^s <= 2^13."""
+    if not bound > 0 or not math.isfinite(bound):
+        return 0
+    return max(-60, min(60, int(math.floor(math.log2(8192.0 / (1.25 * bound))))))
+
+
+def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, B, N, max_retries=2):
+    """The discrete adjoint on the tensor cores (lime_lindblad_adjoint_stream)."""
+    lib = nat.require_device()
+    dev = heff.device
+    C = gsrc.shape[0]
+    heff_adj = (-heff.mH).contiguous()
+    m_adj = None if m is None else m.conj().contiguous()
+    shared = heff.shape[0] == 1
+    G = 1 if shared else B
+    # rho is scaled by its largest element over the checkpoints (the
+    # evolution contracts); the adjoint stage inputs are scaled per step on
+    # the device from max |lam|
+    pmax = float(torch.view_as_real(ckpts).abs().max().item())
+    sb = _pow2_scale(pmax)
+    wsb = lib.lime_lindblad_adjoint_stream_workspace(N, C, G, K)
+    ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
+    aligned = (ws.data_ptr() + 1023) // 1024 * 1024
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    for attempt in range(max_retries + 1):
+        gd = torch.zeros((C, N), dtype=torch.float64, device=dev)
+        gb = torch.zeros((C, max(N - 1, 1)), dtype=torch.float64, device=dev)
+        gg = torch.zeros((C, N), dtype=torch.float64, device=dev)
+        status.zero_()
+        d = nat.AdjointStreamDesc()
+        d.n, d.batch, d.param_batch, d.n_steps, d.seg_steps = N, C, B, n_steps, K
+        d.n_obs, d.obs_every = n_obs, obs_every
+        d.scale_b_log2, d.scale_l_log2 = sb, 0
+        d.dt = float(dt)
+        d.ckpt = ckpts.data_ptr()
+        d.heff, d.heff_stride = heff.data_ptr(), (0 if shared else N * N)
+        d.heff_adj, d.heff_adj_stride = heff_adj.data_ptr(), (0 if shared else N * N)
+        if m is not None:
+            d.m, d.m_adj = m.data_ptr(), m_adj.data_ptr()
+            d.m_stride = 0 if m.shape[0] == 1 else N * N
+        if n_obs > 0:
+            d.obs_ops, d.obs_stride = Et.data_ptr(), (0 if Et.shape[0] == 1 else n_obs * N * N)
+            d.obs_grad = gsrc.data_ptr()
+        d.grad_diag, d.grad_bond, d.grad_gamma = gd.data_ptr(), gb.data_ptr(), gg.data_ptr()
+        d.workspace, d.workspace_bytes = aligned, wsb
+        d.status = status.data_ptr()
+        nat.check(lib.lime_lindblad_adjoint_stream(d, torch.cuda.current_stream().cuda_stream),
+                  'lime_lindblad_adjoint_stream')
+        flags = int(status.item())
+        if flags & nat.LIME_FLAG_RANGE and attempt < max_retries:
+            sb -= 2
+            continue
+        if flags:
+            raise nat.KernelFlagError(flags, 'chain_observables backward (split)')
+        return gd, gb, gg
+
+
 class _ChainObservables(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, eps, bond, gamma, H0, rho0, E, dt, n_steps, site0, obs_every, checkpoint):
+    def forward(ctx, eps, bond, gamma, H0, rho0, E, dt, n_steps, site0, obs_every, checkpoint, precision):
         dev = eps.device
         B, ns = eps.shape
         N = H0.shape[-1]
@@ -71,28 +157,38 @@ class _ChainObservables(torch.autograd.Function):
         ckpt0 = work.clone()
         obs = engine.prepare_obs(list(E), N, B, dev)
         K = max(1, min(checkpoint, n_steps))
-        o, states, status = engine._run_f64(gen, work, dt, n_steps, obs, obs_every, K, 0.0,
-                                            param_batch=B)
-        flags = int(status.item())
-        if flags:
-            raise nat.KernelFlagError(flags, 'chain_observables forward')
+        if precision == 'split':
+            if K % obs_every:
+                raise ValueError('precision="split" needs checkpoint to be a multiple of obs_every')
+            o, states = _forward_split(gen, work, dt, n_steps, list(E), obs_every, B, K)
+            Ed = torch.stack([e.to(CDT) for e in E], 0).unsqueeze(0).contiguous() if len(E) else None
+            obs = (Ed, len(E), 0, 0)
+        else:
+            o, states, status = engine._run_f64(gen, work, dt, n_steps, obs, obs_every, K, 0.0,
+                                                param_batch=B)
+            flags = int(status.item())
+            if flags:
+                raise nat.KernelFlagError(flags, 'chain_observables forward')
         if not herm:
             o_out = o[:B] + 1j * o[B:]
         else:
             o_out = o
         ctx.save_for_backward(gen.heff, gen.m, ckpt0, states, obs[0])
-        ctx.meta = (B, N, ns, herm, dt, n_steps, site0, obs_every, K, obs[1], obs[2], obs[3])
+        ctx.meta = (B, N, ns, herm, dt, n_steps, site0, obs_every, K, obs[1], obs[2], obs[3], precision)
         return o_out.clone()
 
     @staticmethod
     def backward(ctx, g):
         heff, m, ckpt0, states, Et = ctx.saved_tensors
-        B, N, ns, herm, dt, n_steps, site0, obs_every, K, n_obs, obs_diag, obs_stride = ctx.meta
+        B, N, ns, herm, dt, n_steps, site0, obs_every, K, n_obs, obs_diag, obs_stride, precision = ctx.meta
         lib = nat.require_device()
         dev = heff.device
         g = g.to(CDT).contiguous()
         gsrc = g if herm else torch.cat([g, -1j * g], 0).contiguous()
         C = gsrc.shape[0]                       # number of Hermitian chains x B
+        if precision == 'split':
+            gd, gb, gg = _backward_split(heff, m, states, gsrc, Et, n_obs, dt, n_steps, obs_every, K, B, N)
+            return _finish_grads(gd, gb, gg, herm, B, ns, site0)
         heff_adj = (-heff.mH).contiguous()
         m_adj = None if m is None else m.conj().contiguous()
         lam = torch.zeros((C, N, N), dtype=CDT, device=dev)
@@ -124,15 +220,19 @@ class _ChainObservables(torch.autograd.Function):
             d.workspace, d.workspace_bytes = ws.data_ptr(), wsb
             nat.check(lib.lime_lindblad_adjoint_f64(d, torch.cuda.current_stream().cuda_stream),
                       'lime_lindblad_adjoint_f64')
-        if not herm:
-            gd = gd[:B] + gd[B:]
-            gb = gb[:B] + gb[B:]
-            gg = gg[:B] + gg[B:]
-        sl = slice(site0, site0 + ns)
-        g_eps = gd[:, sl]
-        g_bond = gb[:, site0:site0 + ns - 1] if ns > 1 else gb[:, :0]
-        g_gamma = gg[:, sl]
-        return g_eps, g_bond, g_gamma, None, None, None, None, None, None, None, None
+        return _finish_grads(gd, gb, gg, herm, B, ns, site0)
+
+
+def _finish_grads(gd, gb, gg, herm, B, ns, site0):
+    if not herm:
+        gd = gd[:B] + gd[B:]
+        gb = gb[:B] + gb[B:]
+        gg = gg[:B] + gg[B:]
+    sl = slice(site0, site0 + ns)
+    g_eps = gd[:, sl]
+    g_bond = gb[:, site0:site0 + ns - 1] if ns > 1 else gb[:, :0]
+    g_gamma = gg[:, sl]
+    return g_eps, g_bond, g_gamma, None, None, None, None, None, None, None, None, None
 
 
 def chain_observables(H0, eps, bond, gamma, rho0, e_ops, dt: float, n_steps: int, site0: int = 0,
@@ -146,8 +246,8 @@ def chain_observables(H0, eps, bond, gamma, rho0, e_ops, dt: float, n_steps: int
     Returns (B, n_steps // obs_every, n_obs) complex128 with observable k
     recorded after step (k + 1) obs_every - 1.
     """
-    if precision != 'fp64':
-        raise ValueError('chain_observables differentiates the FP64 path (precision="fp64")')
+    if precision not in ('fp64', 'split'):
+        raise ValueError("precision must be 'fp64' or 'split'")
     dev = eps.device
     H0 = engine.as_device(H0, dev)
     if H0.dim() == 2:
@@ -155,4 +255,4 @@ def chain_observables(H0, eps, bond, gamma, rho0, e_ops, dt: float, n_steps: int
     rho0 = engine.as_device(rho0, dev)
     E = [engine.as_device(e, dev) for e in e_ops]
     return _ChainObservables.apply(eps, bond, gamma, H0, rho0, E, float(dt), int(n_steps), int(site0),
-                                   int(obs_every), int(checkpoint))
+                                   int(obs_every), int(checkpoint), precision)

@@ -51,6 +51,9 @@ struct Args {
   float* Acc;
   const double2* m;                   // [P|1][n][n] or null
   int64_t m_stride;
+  bool keep_s;                        // maintain the fp32 stage-input copy (Sc / Sn)
+  const int* sb_exp_dev;              // GEMM 1: B scale exponent read from the device (or null: inv_sb)
+  float* stage_store;                 // finish_kernel: also store the stage input here ([B][W][np]) or null
   int32_t* status;
   uint32_t max_wait;
 };
@@ -101,7 +104,7 @@ __device__ __forceinline__ void update8(const Args& a, int b, int jj, int y, con
   const size_t base = (size_t)b * inst_floats(a);
   float sv[8];
   sg::rk4_stage8(a.rk, a.Phi + base, a.Plo + base, a.Acc + base, (size_t)jj * a.np + y, f, sv, bad);
-  if (a.m != nullptr) sg::st8(a.Sn + base + (size_t)jj * a.np + y, sv);
+  if (a.keep_s) sg::st8(a.Sn + base + (size_t)jj * a.np + y, sv);
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     sv[i] = __fmul_rn(sv[i], a.sb);
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
   T.c0 = 0;
   T.n_chunks = KC;
   T.row_inv = (kZ ? a.rinv2 : a.rinv1) + ((size_t)g * MT + mt) * kBM;
-  T.inv_sb = kZ ? a.inv_sy : a.inv_sb;
+  T.inv_sb = kZ ? a.inv_sy : (a.sb_exp_dev != nullptr ? ldexpf(1.f, -*a.sb_exp_dev) : a.inv_sb);
   T.max_wait = a.max_wait;
   const float* ft = S.tile();
   if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
@@ -213,6 +216,12 @@ __global__ void finish_kernel(Args a, int batch) {
     const int rem = (int)(q % runs);
     const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
     float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (a.stage_store != nullptr) {
+      const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
+      float sc[8];
+      sg::ld8(a.Sc + e, sc);
+      sg::st8(a.stage_store + e, sc);
+    }
     assemble_f(a, b, jj, y, f);
     update8(a, b, jj, y, f, bad, range);
   }
@@ -282,7 +291,7 @@ __global__ void init_kernel(Args a, const double2* rho, int batch) {
     const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
     sg::st8(a.Phi + e, hv);
     sg::st8(a.Plo + e, lv);
-    if (a.m != nullptr) sg::st8(a.Sn + e, hv);
+    if (a.keep_s) sg::st8(a.Sn + e, hv);
     const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
     sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, x, im, sv);
   }
@@ -320,6 +329,230 @@ __global__ void final_kernel(Args a, double2* rho, int batch) {
     const size_t base = (size_t)b * inst_floats(a);
     const size_t er = base + (size_t)x * a.np + y, ei = base + (size_t)(a.np + x) * a.np + y;
     rho[q] = make_double2((double)a.Phi[er] + (double)a.Plo[er], (double)a.Phi[ei] + (double)a.Plo[ei]);
+  }
+}
+
+// ---------------------------------------------------------------- discrete adjoint
+// Backward pass of the RK4 steps above (the FP64 adjoint kernel's recursion,
+// lime_lindblad_adjoint_f64): per step, with lam the adjoint state after the
+// step and ab_i the inputs of the adjoint generator L^dag(x) = -i(G x -
+// x G^dag) + conj(M) o x (G = -Heff^dag, run through the same GEMM 1 and
+// assemble_f with the adjoint operands):
+//   ab_4 = dt/6 lam;           yb_4 = L^dag ab_4
+//   ab_3 = dt/3 lam + dt yb_4;  ab_2 = dt/3 lam + dt/2 yb_3;  ab_1 = dt/6 lam + dt/2 yb_2
+//   lam <- lam + yb_4 + yb_3 + yb_2 + yb_1
+// and the parameter gradients pair ab_i with the forward stage input y_i.
+struct AdjState {
+  float* Lhi;        // [B][W][np] adjoint state (fp32 pair, compensated)
+  float* Llo;
+  float* LAcc;       // sum of the yb of the current step
+  unsigned* lmax;    // device: max |lam| of the current step (float bits)
+  int* sl_exp;       // device: exponent of the adjoint B scale for the current step
+  float bound;       // |ab| <= bound * max |lam| (dt/2: ab_i = c lam + c' yb)
+};
+
+// Per step, the adjoint stage inputs are scaled by the power of two that puts
+// bound * max |lam| at 2^13 / 1.25 (lam changes by orders of magnitude over a
+// backward pass, one scale for all steps would waste the fixed-point range).
+__global__ void adj_scale_kernel(AdjState j) {
+  const float m = __uint_as_float(*j.lmax) * j.bound;
+  int e = 0;
+  if (m > 0.f && isfinite(m)) {
+    e = (int)floorf(log2f(6553.6f / m));
+    e = e < -60 ? -60 : (e > 60 ? 60 : e);
+  }
+  *j.sl_exp = e;
+  *j.lmax = 0u;
+}
+
+// Source of the observables recorded after this step, lam += Herm(g E^dag)
+// (torch's convention dL = Re sum conj(g) d obs), and max |lam| of the step.
+__global__ void adj_source_kernel(Args a, AdjState j, int batch, const double2* E, int64_t e_stride, int n_obs,
+                                  const double2* gsrc, int n_slots, int slot) {
+  const size_t runs = (size_t)a.W * (a.np / 8);
+  const size_t total = (size_t)batch * runs;
+  float mx = 0.f;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / runs);
+    const int rem = (int)(q % runs);
+    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
+    const bool im = jj >= a.np;
+    const int x = im ? jj - a.np : jj;
+    const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
+    float hi[8];
+    sg::ld8(j.Lhi + e, hi);
+    if (slot >= 0 && x < a.n) {
+      float lo[8];
+      sg::ld8(j.Llo + e, lo);
+      const double2* Eb = E + (e_stride ? (int64_t)(b % a.P) * e_stride : 0);
+      const double2* g = gsrc + ((size_t)b * n_slots + slot) * n_obs;
+#pragma unroll 1
+      for (int i = 0; i < 8; ++i) {
+        const int row = y + i;
+        if (row >= a.n) break;
+        double sr = 0.0, si = 0.0;
+        for (int o = 0; o < n_obs; ++o) {
+          const double2* Eo = Eb + (int64_t)o * a.n * a.n;
+          const double2 eji = Eo[(size_t)x * a.n + row], eij = Eo[(size_t)row * a.n + x], gv = g[o];
+          // (g conj(E_ji) + conj(g) E_ij) / 2
+          sr += 0.5 * ((gv.x * eji.x + gv.y * eji.y) + (gv.x * eij.x + gv.y * eij.y));
+          si += 0.5 * ((gv.y * eji.x - gv.x * eji.y) + (gv.x * eij.y - gv.y * eij.x));
+        }
+        const float src = (float)(im ? si : sr);
+        hi[i] = rk4_final_f32(hi[i], 0.f, src, 1.f, 0.f, lo[i]);
+      }
+      sg::st8(j.Lhi + e, hi);
+      sg::st8(j.Llo + e, lo);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) mx = fmaxf(mx, fabsf(hi[i]));
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(j.lmax, __float_as_uint(mx));
+}
+
+// ab_4 = dt/6 lam as the next GEMM 1 input (fp32 copy and scaled B pieces).
+__global__ void adj_start_kernel(Args a, AdjState j, int batch, float dt6) {
+  const size_t runs = (size_t)a.W * (a.np / 8);
+  const size_t total = (size_t)batch * runs;
+  const float sl = ldexpf(1.f, *j.sl_exp);
+  bool range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / runs);
+    const int rem = (int)(q % runs);
+    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
+    const bool im = jj >= a.np;
+    const int x = im ? jj - a.np : jj;
+    const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
+    float ab[8];
+    sg::ld8(j.Lhi + e, ab);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) ab[i] = __fmul_rn(dt6, ab[i]);
+    sg::st8(a.Sn + e, ab);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      ab[i] = __fmul_rn(ab[i], sl);
+      range |= !(fabsf(ab[i]) <= sg::kBMax);
+    }
+    const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
+    sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, x, im, ab);
+  }
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// yb_i = L^dag ab_i (Xg = G ab_i from GEMM 1, ab_i in Sc) and the next
+// adjoint stage input (stage i = 4, 3, 2) or the new lam (i = 1).
+__global__ void adj_finish_kernel(Args a, AdjState j, int batch, int stage_i, float c_l, float c_y) {
+  const size_t runs = (size_t)a.W * (a.np / 8);
+  const size_t total = (size_t)batch * runs;
+  const float sl = ldexpf(1.f, *j.sl_exp);
+  bool range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / runs);
+    const int rem = (int)(q % runs);
+    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
+    const bool im = jj >= a.np;
+    const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
+    float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    assemble_f(a, b, jj, y, f);
+    float acc[8], hi[8];
+    if (stage_i == 4) {
+      sg::st8(j.LAcc + e, f);
+    } else {
+      sg::ld8(j.LAcc + e, acc);
+      if (stage_i > 1) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i] = __fadd_rn(acc[i], f[i]);
+        sg::st8(j.LAcc + e, acc);
+      } else {
+        float lo[8];
+        sg::ld8(j.Lhi + e, hi);
+        sg::ld8(j.Llo + e, lo);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) hi[i] = rk4_final_f32(hi[i], acc[i], f[i], 1.f, 0.f, lo[i]);
+        sg::st8(j.Lhi + e, hi);
+        sg::st8(j.Llo + e, lo);
+      }
+    }
+    if (stage_i > 1) {
+      float nx[8];
+      sg::ld8(j.Lhi + e, hi);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) nx[i] = __fmaf_rn(c_l, hi[i], __fmul_rn(c_y, f[i]));
+      sg::st8(a.Sn + e, nx);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        nx[i] = __fmul_rn(nx[i], sl);
+        range |= !(fabsf(nx[i]) <= sg::kBMax);
+      }
+      const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
+      sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, im ? jj - a.np : jj, im, nx);
+    }
+  }
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// Gradient contributions of one stage for the chain model (site energies on
+// the diagonal, nearest-neighbour bonds, site dephasing rates), pairing the
+// adjoint stage input ab with the forward stage input y (both Hermitian):
+//   d/dH_kk   += 2 sum_x Im(conj(ab_kx) y_kx)
+//   d/dJ_k    += 2 sum_x Im(conj(ab_kx) y_k+1,x) + Im(conj(ab_k+1,x) y_kx)
+//   d/dgamma_k -= sum_{x != k} Re(conj(ab_kx) y_kx)
+// One block per (instance, run of 8 rows), threads over the columns.
+__global__ void adj_grad_kernel(Args a, const float* ab, const float* yst, int batch, double* gd, double* gb,
+                                double* gg) {
+  const int runs = a.np / 8;
+  const int b = blockIdx.x / runs, k0 = (blockIdx.x % runs) * 8;
+  if (b >= batch || k0 >= a.n) return;
+  const int n = a.n, np = a.np;
+  const float* A = ab + (size_t)b * inst_floats(a);
+  const float* Y = yst + (size_t)b * inst_floats(a);
+  double part[24];
+#pragma unroll
+  for (int i = 0; i < 24; ++i) part[i] = 0.0;
+  for (int x = threadIdx.x; x < n; x += blockDim.x) {
+    float ar[9], ai[9], yr[9], yi[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const int k = k0 + i;
+      const bool ok = k < np;
+      ar[i] = ok ? A[(size_t)x * np + k] : 0.f;
+      ai[i] = ok ? A[(size_t)(np + x) * np + k] : 0.f;
+      yr[i] = ok ? Y[(size_t)x * np + k] : 0.f;
+      yi[i] = ok ? Y[(size_t)(np + x) * np + k] : 0.f;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int k = k0 + i;
+      if (k < n) {
+        part[i] += 2.0 * ((double)ar[i] * yi[i] - (double)ai[i] * yr[i]);
+        if (x != k) part[16 + i] -= (double)ar[i] * yr[i] + (double)ai[i] * yi[i];
+        if (k + 1 < n)
+          part[8 + i] += 2.0 * (((double)ar[i] * yi[i + 1] - (double)ai[i] * yr[i + 1]) +
+                                ((double)ar[i + 1] * yi[i] - (double)ai[i + 1] * yr[i]));
+      }
+    }
+  }
+  __shared__ double red[4][24];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int i = 0; i < 24; ++i) {
+    double v = part[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) red[w][i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 24) {
+    const int i = threadIdx.x;
+    double v = 0.0;
+    for (int ww = 0; ww < (int)(blockDim.x >> 5); ++ww) v += red[ww][i];
+    const int k = k0 + (i & 7);
+    const int nb = n > 1 ? n - 1 : 1;
+    if (k < n) {
+      if (i < 8) atomicAdd(gd + (size_t)b * n + k, v);
+      else if (i < 16) { if (k + 1 < n) atomicAdd(gb + (size_t)b * nb + k, v); }
+      else atomicAdd(gg + (size_t)b * n + k, v);
+    }
   }
 }
 
@@ -416,6 +649,9 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
                  (float)(d->dt / 6.0 - (double)(float)(d->dt / 6.0))};
   a.m = reinterpret_cast<const double2*>(d->m);
   a.m_stride = d->m_stride;
+  a.keep_s = a.m != nullptr;
+  a.stage_store = nullptr;
+  a.sb_exp_dev = nullptr;
   a.status = d->status;
   a.max_wait = 1u << 26;
   int64_t launches = 0;
@@ -472,6 +708,180 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   lsm::final_kernel<<<fb, 256, 0, st>>>(a, reinterpret_cast<double2*>(d->rho), B);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
+  count_launch(launches);
+  return LIME_OK;
+}
+
+
+extern "C" size_t lime_lindblad_adjoint_stream_workspace(int32_t n, int32_t batch, int32_t n_generators,
+                                                         int32_t seg_steps) {
+  if (n <= 0 || batch <= 0 || n_generators <= 0 || seg_steps <= 0) return 0;
+  const LsmLayout L = lsm_layout(n, batch, n_generators, 0);
+  return L.total + 3 * L.a1 + L.r1 + 3 * L.st + 1024 + 4 * (size_t)seg_steps * L.st;
+}
+
+extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc* d, void* stream) {
+  if (!d || d->n <= 0 || d->batch <= 0 || d->n_steps <= 0 || d->seg_steps <= 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (!d->ckpt || !d->heff || !d->heff_adj || !d->grad_diag || !d->grad_bond || !d->grad_gamma) return LIME_ERR_ARG;
+  if (!d->workspace || !d->status) return LIME_ERR_ARG;
+  if (d->n_obs > 0 && (!d->obs_ops || !d->obs_grad)) return LIME_ERR_ARG;
+  if ((d->m == nullptr) != (d->m_adj == nullptr)) return LIME_ERR_ARG;
+  if (d->heff_stride < 0 || d->heff_adj_stride < 0 || d->m_stride < 0 || d->obs_stride < 0) return LIME_ERR_ARG;
+  if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60 || d->scale_l_log2 < -60 || d->scale_l_log2 > 60)
+    return LIME_ERR_ARG;
+  if (d->n > 4096) return LIME_ERR_UNSUPPORTED;
+  const int P = d->param_batch > 0 ? d->param_batch : d->batch;
+  if (P > d->batch) return LIME_ERR_ARG;
+  const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  const int G = (d->heff_stride == 0 && d->heff_adj_stride == 0) ? 1 : P;
+  const int seg = d->seg_steps;
+  if (d->workspace_bytes < lime_lindblad_adjoint_stream_workspace(d->n, d->batch, G, seg)) return LIME_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
+  const LsmLayout L = lsm_layout(d->n, d->batch, G, 0);
+  const int B = d->batch;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
+  lsm::Args af{};
+  af.n = d->n; af.np = L.np; af.W = L.W; af.NT = L.NT; af.K = 0; af.P = P; af.G = G;
+  af.KC1 = L.KC1; af.KC2 = 0; af.MT1 = L.MT1; af.MT2 = 0;
+  for (int i = 0; i < 3; ++i) { af.A1[i] = w; w += L.a1; }
+  for (int i = 0; i < 3; ++i) { af.A2[i] = w; w += L.a2; }
+  af.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
+  af.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
+  uint8_t* B1[2][2];
+  for (int bb = 0; bb < 2; ++bb)
+    for (int i = 0; i < 2; ++i) { B1[bb][i] = w; w += L.b1; }
+  for (int i = 0; i < 2; ++i) { af.B2[i] = w; w += L.b2; }
+  af.Xg = reinterpret_cast<float*>(w); w += L.st;
+  float* Sbuf[2];
+  for (int i = 0; i < 2; ++i) { Sbuf[i] = reinterpret_cast<float*>(w); w += L.st; }
+  af.Phi = reinterpret_cast<float*>(w); w += L.st;
+  af.Plo = reinterpret_cast<float*>(w); w += L.st;
+  af.Acc = reinterpret_cast<float*>(w); w += L.st;
+  w = reinterpret_cast<uint8_t*>(d->workspace) + L.total;   // past the forward layout (and its slack)
+  lsm::Args aa = af;                                          // the adjoint generator: own A pieces
+  for (int i = 0; i < 3; ++i) { aa.A1[i] = w; w += L.a1; }
+  aa.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
+  lsm::AdjState J{};
+  J.Lhi = reinterpret_cast<float*>(w); w += L.st;
+  J.Llo = reinterpret_cast<float*>(w); w += L.st;
+  J.LAcc = reinterpret_cast<float*>(w); w += L.st;
+  J.lmax = reinterpret_cast<unsigned*>(w);
+  J.sl_exp = reinterpret_cast<int*>(w + 4);
+  w += 1024;
+  float* store = reinterpret_cast<float*>(w);                 // [seg][4][B][W][np]
+  const size_t inst = (size_t)L.W * L.np;
+
+  af.sb = ldexpf(1.f, d->scale_b_log2);
+  af.inv_sb = ldexpf(1.f, -d->scale_b_log2);
+  aa.sb = aa.inv_sb = 1.f;                                    // (per step: J.sl_exp)
+  J.bound = (float)(d->dt / 2.0);
+  af.rk = sg::RK4{0, (float)(d->dt / 2.0), (float)d->dt, (float)(d->dt / 6.0),
+                  (float)(d->dt / 6.0 - (double)(float)(d->dt / 6.0))};
+  af.m = reinterpret_cast<const double2*>(d->m);
+  aa.m = reinterpret_cast<const double2*>(d->m_adj);
+  af.m_stride = aa.m_stride = d->m_stride;
+  af.keep_s = aa.keep_s = true;
+  af.sb_exp_dev = nullptr;
+  aa.sb_exp_dev = J.sl_exp;
+  af.stage_store = aa.stage_store = nullptr;
+  af.status = aa.status = d->status;
+  af.max_wait = aa.max_wait = 1u << 26;
+  int64_t launches = 0;
+
+  const int per_g = L.MT1 * 128;
+  lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
+                                                  nullptr, 0, af);
+  LIME_CUDA_TRY(cudaGetLastError());
+  lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff_adj),
+                                                  d->heff_adj_stride, nullptr, 0, aa);
+  LIME_CUDA_TRY(cudaGetLastError());
+  launches += 2;
+  LIME_CUDA_TRY(cudaMemsetAsync(J.Lhi, 0, 2 * L.st, st));   // Lhi and Llo
+  LIME_CUDA_TRY(cudaMemsetAsync(J.lmax, 0, 8, st));          // lmax and sl_exp
+  const size_t smem = sg::kSmemBytes;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t runs = (size_t)B * L.W * (L.np / 8);
+  const int eb = (int)((runs + 255) / 256 < 65535 ? (runs + 255) / 256 : 65535);
+  const int gemm_grid = B * L.MT1 * L.NT;
+  const int n_slots = d->n_steps / obs_every;
+  const int n_seg = (d->n_steps + seg - 1) / seg;
+  const double dt = d->dt;
+
+  for (int sgi = n_seg - 1; sgi >= 0; --sgi) {
+    const int s0 = sgi * seg;
+    const int len = (d->n_steps - s0 < seg) ? d->n_steps - s0 : seg;
+    // ---- forward recompute of the segment, storing every stage input
+    int cur = 0;
+    af.B1n[0] = B1[0][0]; af.B1n[1] = B1[0][1];
+    af.Sn = Sbuf[0];
+    lsm::init_kernel<<<eb, 256, 0, st>>>(af, reinterpret_cast<const double2*>(d->ckpt) + (size_t)sgi * B * d->n * d->n,
+                                         B);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+    for (int s = 0; s < len; ++s) {
+      for (int k = 0; k < 4; ++k) {
+        af.rk.stage = k;
+        af.B1c[0] = B1[cur][0]; af.B1c[1] = B1[cur][1];
+        af.B1n[0] = B1[cur ^ 1][0]; af.B1n[1] = B1[cur ^ 1][1];
+        af.Sc = Sbuf[cur];
+        af.Sn = Sbuf[cur ^ 1];
+        af.stage_store = store + ((size_t)s * 4 + k) * B * inst;
+        lsm::gemm_kernel<false><<<gemm_grid, sg::kThreads, smem, st>>>(af);
+        LIME_CUDA_TRY(cudaGetLastError());
+        lsm::finish_kernel<<<eb, 256, 0, st>>>(af, B);
+        LIME_CUDA_TRY(cudaGetLastError());
+        launches += 2;
+        cur ^= 1;
+      }
+    }
+    af.stage_store = nullptr;
+    // ---- backward through the segment
+    int c = 0;
+    for (int s = len - 1; s >= 0; --s) {
+      const int gstep = s0 + s;
+      const int slot = (d->n_obs > 0 && ((gstep + 1) % obs_every) == 0) ? (gstep + 1) / obs_every - 1 : -1;
+      aa.B1n[0] = B1[c][0]; aa.B1n[1] = B1[c][1];
+      aa.Sn = Sbuf[c];
+      lsm::adj_source_kernel<<<eb, 256, 0, st>>>(aa, J, B, reinterpret_cast<const double2*>(d->obs_ops),
+                                                  d->obs_stride, d->n_obs,
+                                                  reinterpret_cast<const double2*>(d->obs_grad), n_slots, slot);
+      LIME_CUDA_TRY(cudaGetLastError());
+      lsm::adj_scale_kernel<<<1, 1, 0, st>>>(J);
+      LIME_CUDA_TRY(cudaGetLastError());
+      lsm::adj_start_kernel<<<eb, 256, 0, st>>>(aa, J, B, (float)(dt / 6.0));
+      LIME_CUDA_TRY(cudaGetLastError());
+      launches += 3;
+      for (int i = 4; i >= 1; --i) {
+        aa.B1c[0] = B1[c][0]; aa.B1c[1] = B1[c][1];
+        aa.Sc = Sbuf[c];
+        aa.B1n[0] = B1[c ^ 1][0]; aa.B1n[1] = B1[c ^ 1][1];
+        aa.Sn = Sbuf[c ^ 1];
+        lsm::gemm_kernel<false><<<gemm_grid, sg::kThreads, smem, st>>>(aa);
+        LIME_CUDA_TRY(cudaGetLastError());
+        lsm::adj_grad_kernel<<<B * (L.np / 8), 128, 0, st>>>(aa, Sbuf[c], store + ((size_t)s * 4 + (i - 1)) * B * inst,
+                                                             B, d->grad_diag, d->grad_bond, d->grad_gamma);
+        LIME_CUDA_TRY(cudaGetLastError());
+        const float c_l = (float)(i == 2 ? dt / 6.0 : dt / 3.0);
+        const float c_y = (float)(i == 4 ? dt : dt / 2.0);
+        lsm::adj_finish_kernel<<<eb, 256, 0, st>>>(aa, J, B, i, c_l, c_y);
+        LIME_CUDA_TRY(cudaGetLastError());
+        launches += 3;
+        if (i > 1) c ^= 1;
+      }
+    }
+  }
+  if (d->lam) {
+    lsm::Args al = af;
+    al.Phi = J.Lhi;
+    al.Plo = J.Llo;
+    const size_t tot = (size_t)B * d->n * d->n;
+    const int fb = (int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535);
+    lsm::final_kernel<<<fb, 256, 0, st>>>(al, reinterpret_cast<double2*>(d->lam), B);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+  }
   count_launch(launches);
   return LIME_OK;
 }

@@ -111,6 +111,7 @@ def _c_layout(struct_name, fields):
     ('LimeRedfieldRK4Desc', 'RedfieldRK4Desc'),
     ('LimeRedfieldSplitDesc', 'RedfieldSplitDesc'),
     ('LimeLindbladStreamDesc', 'LindbladStreamDesc'),
+    ('LimeLindbladAdjointStreamDesc', 'AdjointStreamDesc'),
 ])
 def test_descriptor_layout_matches_c(tmp_path, cname, pyname):
     from lime_gb300 import _native

@@ -147,3 +147,50 @@ def test_checkpoint_interval_does_not_change_gradients():
         obs.real.sum().backward()
         out.append(eps.grad.cpu().numpy())
     assert rel(out[0], out[2]) < 1e-12 and rel(out[1], out[2]) < 1e-12
+
+
+def _grads(c, precision, dt, n_steps, K, w=None):
+    from lime_gb300.adjoint import chain_observables
+    eps = c['eps'].clone().requires_grad_(True)
+    bond = c['bond'].clone().requires_grad_(True)
+    gamma = c['gamma'].clone().requires_grad_(True)
+    obs = chain_observables(c['H0'], eps, bond, gamma, c['rho0'], c['E'], dt, n_steps,
+                            site0=c['site0'], checkpoint=K, precision=precision)
+    if w is None:
+        g = torch.Generator(device='cpu').manual_seed(7)
+        w = torch.complex(torch.randn(obs.shape, generator=g, dtype=torch.float64),
+                          torch.randn(obs.shape, generator=g, dtype=torch.float64)).to(obs.device)
+    _loss(obs, w).backward()
+    return obs.detach().cpu().numpy(), [eps.grad.cpu().numpy(), bond.grad.cpu().numpy(),
+                                        gamma.grad.cpu().numpy()], w
+
+
+@pytest.mark.parametrize('case', ['population', 'absorption'])
+def test_split_adjoint_matches_fp64_adjoint(case):
+    """Tensor-core adjoint (streaming split-precision GEMMs) against the FP64
+    adjoint, which the test above pins to autograd and finite differences."""
+    dev = torch.device('cuda')
+    c = _setup_population(dev) if case == 'population' else _setup_absorption(dev)
+    o64, g64, w = _grads(c, 'fp64', 0.05, 37, 8)
+    osp, gsp, _ = _grads(c, 'split', 0.05, 37, 8, w)
+    assert rel(osp, o64) < 1e-6
+    for got, ref in zip(gsp, g64):
+        assert rel(got, ref) < GTOL, (case, rel(got, ref))
+
+
+def test_split_adjoint_large_chain():
+    """n = 70 (> 64): the forward runs on the streaming path too."""
+    dev = torch.device('cuda')
+    n, B = 70, 2
+    rng = np.random.default_rng(17)
+    c = dict(eps=torch.tensor(rng.normal(0, 0.05, (B, n)), device=dev),
+             bond=torch.tensor(-0.1 + 0.01 * rng.normal(size=(B, n - 1)), device=dev),
+             gamma=torch.tensor(rng.uniform(0.005, 0.05, (B, n)), device=dev),
+             H0=torch.zeros((n, n), dtype=torch.complex128, device=dev),
+             rho0=torch.as_tensor(chains.ground_dm(n), device=dev),
+             E=[torch.as_tensor(p, device=dev) for p in chains.population_ops(n)[:3]], site0=0)
+    o64, g64, w = _grads(c, 'fp64', 0.05, 12, 4)
+    osp, gsp, _ = _grads(c, 'split', 0.05, 12, 4, w)
+    assert rel(osp, o64) < 1e-6
+    for got, ref in zip(gsp, g64):
+        assert rel(got, ref) < GTOL, rel(got, ref)
