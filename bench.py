@@ -348,8 +348,10 @@ def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=
     """Adjoint/forward cost on the differentiated absorption workload shape:
     129-dim chains (|g> + 128 sites), 256 disorder samples, dipole
     correlation <mu(t) mu(0)>, gradients w.r.t. every site energy, the bond
-    couplings and the dephasing rates, checkpoint every 64 steps.  Times a
-    sample of ``steps`` RK4 steps (the workload runs 4096) of the FP64 path."""
+    couplings and the dephasing rates, checkpointed segments.  Times a sample
+    of ``steps`` RK4 steps (the workload runs 4096) of the FP64 path and of
+    the tensor-core path, and reports the tensor-core gradients' deviation
+    from the FP64 ones."""
     import numpy as np
     from lime_gb300 import chains
     from lime_gb300.adjoint import chain_observables
@@ -363,30 +365,42 @@ def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=
     rho0 = mu @ torch.as_tensor(w['rho_g'], device=dev)
     E = [mu]
 
-    def fwd(req):
+    def fwd(req, precision):
         e = eps.clone().requires_grad_(req)
         b = bond.clone().requires_grad_(req)
         g = gamma.clone().requires_grad_(req)
         return (e, b, g), chain_observables(H0, e, b, g, rho0, E, dt, steps, site0=1,
-                                            checkpoint=checkpoint)
+                                            checkpoint=checkpoint, precision=precision)
 
-    fwd(False)   # warm
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    ev[0].record()
-    params, obs = fwd(True)
-    ev[1].record()
-    loss = obs.real.sum()   # a linear functional of C(t), as a spectrum is
-    loss.backward()
-    ev[2].record()
-    torch.cuda.synchronize()
-    tf = ev[0].elapsed_time(ev[1]) / 1e3
-    tb = ev[1].elapsed_time(ev[2]) / 1e3
-    return {'workload': 'absorption chain dim %d, %d samples, dipole correlation, grads w.r.t. '
-                        '%d site energies + %d bonds + %d dephasing rates, checkpoint %d'
-                        % (N, batch, n_sites, n_sites - 1, n_sites, checkpoint),
-            'sample_steps': steps, 'path': 'fp64',
-            'forward_s': tf, 'adjoint_s': tb, 'adjoint_over_forward': tb / tf}
+    out = {'workload': 'absorption chain dim %d, %d samples, dipole correlation, grads w.r.t. '
+                       '%d site energies + %d bonds + %d dephasing rates, checkpoint %d'
+                       % (N, batch, n_sites, n_sites - 1, n_sites, checkpoint),
+           'sample_steps': steps}
+    grads = {}
+    for precision in ('fp64', 'split'):
+        fwd(False, precision)   # warm
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        params, obs = fwd(True, precision)
+        ev[1].record()
+        loss = obs.real.sum()   # a linear functional of C(t), as a spectrum is
+        loss.backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        tf = ev[0].elapsed_time(ev[1]) / 1e3
+        tb = ev[1].elapsed_time(ev[2]) / 1e3
+        grads[precision] = [p.grad for p in params]
+        out[precision] = {'forward_s': tf, 'adjoint_s': tb, 'adjoint_over_forward': tb / tf}
+    out['path'] = 'fp64'                       # the headline ratio below is the FP64 one
+    out['forward_s'] = out['fp64']['forward_s']
+    out['adjoint_s'] = out['fp64']['adjoint_s']
+    out['adjoint_over_forward'] = out['fp64']['adjoint_over_forward']
+    out['split_grad_rel_error'] = max(
+        float((a - b).abs().max().item() / max(b.abs().max().item(), 1e-300))
+        for a, b in zip(grads['split'], grads['fp64']))
+    out['split_adjoint_speedup_vs_fp64'] = out['fp64']['adjoint_s'] / out['split']['adjoint_s']
+    return out
 
 
 def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k64=3):

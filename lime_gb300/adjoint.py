@@ -161,7 +161,14 @@ class _ChainObservables(torch.autograd.Function):
             if K % obs_every:
                 raise ValueError('precision="split" needs checkpoint to be a multiple of obs_every')
             o, states = _forward_split(gen, work, dt, n_steps, list(E), obs_every, B, K)
-            Ed = torch.stack([e.to(CDT) for e in E], 0).unsqueeze(0).contiguous() if len(E) else None
+            Ed = None
+            if len(E):
+                # dense observables, per instance (B, n_obs, N, N) when any is batched
+                if any(e.dim() == 3 for e in E):
+                    Ed = torch.stack([(e.expand(B, N, N) if e.dim() == 2 else e).to(CDT) for e in E], 1)
+                else:
+                    Ed = torch.stack([e.to(CDT) for e in E], 0).unsqueeze(0)
+                Ed = Ed.contiguous()
             obs = (Ed, len(E), 0, 0)
         else:
             o, states, status = engine._run_f64(gen, work, dt, n_steps, obs, obs_every, K, 0.0,

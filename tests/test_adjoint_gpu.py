@@ -194,3 +194,26 @@ def test_split_adjoint_large_chain():
     assert rel(osp, o64) < 1e-6
     for got, ref in zip(gsp, g64):
         assert rel(got, ref) < GTOL, rel(got, ref)
+
+
+def test_split_adjoint_per_instance_dipoles():
+    """The absorption workload's generator: per-realisation dipoles (batched
+    observables) and the real loss sum_t Re C(t) of a spectrum."""
+    from lime_gb300.adjoint import chain_observables
+    dev = torch.device('cuda')
+    w = chains.absorption_ensemble(n_sites=9, batch=3, n_steps=24, dt=0.05)
+    N = 10
+    H0 = torch.zeros((N, N), dtype=torch.complex128, device=dev)
+    mu = torch.as_tensor(w['mu'], device=dev)
+    rho0 = mu @ torch.as_tensor(w['rho_g'], device=dev)
+    out = {}
+    for precision in ('fp64', 'split'):
+        eps = torch.tensor(w['eps'], device=dev).requires_grad_(True)
+        bond = torch.full((3, 8), w['J'], dtype=torch.float64, device=dev).requires_grad_(True)
+        gamma = torch.full((3, 9), w['gamma'], dtype=torch.float64, device=dev).requires_grad_(True)
+        obs = chain_observables(H0, eps, bond, gamma, rho0, [mu], 0.05, 24, site0=1, checkpoint=8,
+                                precision=precision)
+        obs.real.sum().backward()
+        out[precision] = [eps.grad.cpu().numpy(), bond.grad.cpu().numpy(), gamma.grad.cpu().numpy()]
+    for got, ref in zip(out['split'], out['fp64']):
+        assert rel(got, ref) < GTOL, rel(got, ref)
