@@ -234,12 +234,14 @@ class Lindblad_solver:
     def correlation_3op_2t(self, rho0, ops, dt, Nt, Ntau):
         """<A(t) B(t+tau) C(t)>, shape (Nt, Ntau) (lime/oqs.py:1268-1299).
 
-        The Nt inner propagations are independent and run as one batch.
+        The Nt inner propagations are independent and run as one batch (on
+        the tensor cores with ``precision='split'``); the single outer
+        trajectory that seeds them is stored step by step, which the FP64
+        path does.
         """
         gen = engine.LindbladGenerator.build(self.H, self.c_ops)
         dev = gen.heff.device
-        _, states, _ = engine.propagate(gen, rho0, dt, Nt, None, states_every=1,
-                                        precision=self.precision)
+        _, states, _ = engine.propagate(gen, rho0, dt, Nt, None, states_every=1, precision='fp64')
         a, b, c = [engine.as_device(o, dev) for o in ops]
         rho_t = states[0]  # (Nt, n, n)
         start = c @ rho_t @ a

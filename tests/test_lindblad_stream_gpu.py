@@ -119,3 +119,21 @@ def test_stream_launch_count():
     torch.cuda.synchronize()
     # convert + init + 2 GEMMs per stage + an observable pass every 2 steps + final
     assert _native.launch_count() - c0 == 2 + 8 * 6 + 3 + 1
+
+
+def test_multi_operator_correlations_split():
+    """The reference's 3- and 4-operator one- and two-time correlations
+    (golden vectors from the reference) on the tensor cores."""
+    from conftest import load_golden
+    from lime_gb300.oqs import Lindblad_solver
+    g = load_golden('correlations_n4')
+    sol = Lindblad_solver(g['H'], c_ops=list(g['c_ops']), precision='split')
+    ops, rho0, dt = list(g['ops']), g['rho0'], float(g['dt'])
+
+    def rel(a, b):
+        return np.max(np.abs(np.asarray(a) - np.asarray(b))) / np.max(np.abs(b))
+
+    assert rel(sol.correlation_3op_1t(rho0, ops[:3], dt=dt, Nt=30), g['c3op_1t']) < TOL
+    assert rel(sol.correlation_4op_1t(rho0, ops, dt, 30), g['c4op_1t']) < TOL
+    assert rel(sol.correlation_3op_2t(rho0, ops[:3], dt, 12, 10), g['c3op_2t']) < TOL
+    assert rel(sol.correlation_4op_2t(rho0, ops, dt, 12, 10), g['c4op_2t']) < TOL
