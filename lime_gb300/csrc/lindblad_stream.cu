@@ -231,8 +231,15 @@ __global__ void finish_kernel(Args a, int batch) {
 
 // A pieces: GEMM 1 rows (R = blk np + y: Heff for blk 0, L_blk otherwise)
 // and GEMM 2 rows (y: [L_1 | ... | L_K] row y).  One block per row.
+struct ConvertOut {
+  uint8_t* A1[3];                     // [G][MT1][KC1] pieces
+  uint8_t* A2[3];                     // [G][MT2][KC2] pieces
+  float* rinv1;                       // [G][MT1 * 128]
+  float* rinv2;                       // [G][MT2 * 128]
+};
+
 __global__ void convert_kernel(const double2* heff, int64_t heff_stride, const double2* l_ops, int64_t l_stride,
-                               Args a) {
+                               Args a, ConvertOut out) {
   const int rows1 = a.MT1 * kBM, rows2 = a.MT2 * kBM;
   const int per_g = rows1 + (a.K > 0 ? rows2 : 0);
   const int g = blockIdx.x / per_g;
@@ -247,9 +254,8 @@ __global__ void convert_kernel(const double2* heff, int64_t heff_stride, const d
       return kk < n ? src[(int64_t)y * n + kk] : make_double2(0.0, 0.0);
     };
     const size_t go = (size_t)g * a.MT1 * a.KC1 * kPiece;
-    sg::convert_row(elem, R, valid, np, np, a.KC1, const_cast<uint8_t*>(a.A1[0]) + go,
-                    const_cast<uint8_t*>(a.A1[1]) + go, const_cast<uint8_t*>(a.A1[2]) + go,
-                    const_cast<float*>(a.rinv1) + (size_t)g * rows1);
+    sg::convert_row(elem, R, valid, np, np, a.KC1, out.A1[0] + go, out.A1[1] + go, out.A1[2] + go,
+                    out.rinv1 + (size_t)g * rows1);
   } else {
     const int y = q - rows1;
     const double2* src = l_ops + (l_stride ? (int64_t)g * l_stride : 0);
@@ -258,9 +264,8 @@ __global__ void convert_kernel(const double2* heff, int64_t heff_stride, const d
       return x < n ? src[(int64_t)k * n * n + (int64_t)y * n + x] : make_double2(0.0, 0.0);
     };
     const size_t go = (size_t)g * a.MT2 * a.KC2 * kPiece;
-    sg::convert_row(elem, y, y < n, a.K * np, a.K * np, a.KC2, const_cast<uint8_t*>(a.A2[0]) + go,
-                    const_cast<uint8_t*>(a.A2[1]) + go, const_cast<uint8_t*>(a.A2[2]) + go,
-                    const_cast<float*>(a.rinv2) + (size_t)g * rows2);
+    sg::convert_row(elem, y, y < n, a.K * np, a.K * np, a.KC2, out.A2[0] + go, out.A2[1] + go, out.A2[2] + go,
+                    out.rinv2 + (size_t)g * rows2);
   }
 }
 
@@ -625,12 +630,13 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
 
   uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
   lsm::Args a{};
+  lsm::ConvertOut co{};
   a.n = d->n; a.np = L.np; a.W = L.W; a.NT = L.NT; a.K = K; a.P = P; a.G = G;
   a.KC1 = L.KC1; a.KC2 = L.KC2; a.MT1 = L.MT1; a.MT2 = L.MT2;
-  for (int i = 0; i < 3; ++i) { a.A1[i] = w; w += L.a1; }
-  for (int i = 0; i < 3; ++i) { a.A2[i] = w; w += L.a2; }
-  a.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
-  a.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
+  for (int i = 0; i < 3; ++i) { a.A1[i] = co.A1[i] = w; w += L.a1; }
+  for (int i = 0; i < 3; ++i) { a.A2[i] = co.A2[i] = w; w += L.a2; }
+  a.rinv1 = co.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
+  a.rinv2 = co.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
   uint8_t* B1[2][2];
   for (int bb = 0; bb < 2; ++bb)
     for (int i = 0; i < 2; ++i) { B1[bb][i] = w; w += L.b1; }
@@ -658,7 +664,7 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
 
   const int per_g = L.MT1 * 128 + (K > 0 ? L.MT2 * 128 : 0);
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
-                                                  reinterpret_cast<const double2*>(d->l_ops), d->l_stride, a);
+                                                  reinterpret_cast<const double2*>(d->l_ops), d->l_stride, a, co);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
   a.B1n[0] = B1[0][0]; a.B1n[1] = B1[0][1];
@@ -743,12 +749,13 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
 
   uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
   lsm::Args af{};
+  lsm::ConvertOut cf{}, ca{};
   af.n = d->n; af.np = L.np; af.W = L.W; af.NT = L.NT; af.K = 0; af.P = P; af.G = G;
   af.KC1 = L.KC1; af.KC2 = 0; af.MT1 = L.MT1; af.MT2 = 0;
-  for (int i = 0; i < 3; ++i) { af.A1[i] = w; w += L.a1; }
-  for (int i = 0; i < 3; ++i) { af.A2[i] = w; w += L.a2; }
-  af.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
-  af.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
+  for (int i = 0; i < 3; ++i) { af.A1[i] = cf.A1[i] = w; w += L.a1; }
+  for (int i = 0; i < 3; ++i) { af.A2[i] = cf.A2[i] = w; w += L.a2; }
+  af.rinv1 = cf.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
+  af.rinv2 = cf.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
   uint8_t* B1[2][2];
   for (int bb = 0; bb < 2; ++bb)
     for (int i = 0; i < 2; ++i) { B1[bb][i] = w; w += L.b1; }
@@ -761,8 +768,8 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
   af.Acc = reinterpret_cast<float*>(w); w += L.st;
   w = reinterpret_cast<uint8_t*>(d->workspace) + L.total;   // past the forward layout (and its slack)
   lsm::Args aa = af;                                          // the adjoint generator: own A pieces
-  for (int i = 0; i < 3; ++i) { aa.A1[i] = w; w += L.a1; }
-  aa.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
+  for (int i = 0; i < 3; ++i) { aa.A1[i] = ca.A1[i] = w; w += L.a1; }
+  aa.rinv1 = ca.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
   lsm::AdjState J{};
   J.Lhi = reinterpret_cast<float*>(w); w += L.st;
   J.Llo = reinterpret_cast<float*>(w); w += L.st;
@@ -792,10 +799,10 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
 
   const int per_g = L.MT1 * 128;
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
-                                                  nullptr, 0, af);
+                                                  nullptr, 0, af, cf);
   LIME_CUDA_TRY(cudaGetLastError());
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff_adj),
-                                                  d->heff_adj_stride, nullptr, 0, aa);
+                                                  d->heff_adj_stride, nullptr, 0, aa, ca);
   LIME_CUDA_TRY(cudaGetLastError());
   launches += 2;
   LIME_CUDA_TRY(cudaMemsetAsync(J.Lhi, 0, 2 * L.st, st));   // Lhi and Llo
