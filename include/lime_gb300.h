@@ -295,6 +295,12 @@ typedef struct {
   double* obs_out;
   void* workspace;        size_t workspace_bytes;
   int32_t* status;
+  /* driven generator, as in LimeLindbladDesc: Heff(t) = Heff - sum_q
+   * drive_coef[k][q] drive_ops[q] during step k (rebuilt and re-split on
+   * the device every step); n_drive = 0 for a static generator */
+  int32_t n_drive;
+  const double* drive_ops;
+  const double* drive_coef;
 } LimeLindbladStreamDesc;
 
 size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops);

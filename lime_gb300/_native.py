@@ -144,7 +144,8 @@ class LindbladStreamDesc(ctypes.Structure):
                 ('obs_ops', c_void_p), ('obs_stride', c_int64),
                 ('obs_out', c_void_p),
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
-                ('status', c_void_p)]
+                ('status', c_void_p),
+                ('n_drive', c_int32), ('drive_ops', c_void_p), ('drive_coef', c_void_p)]
 
 
 class AdjointStreamDesc(ctypes.Structure):

@@ -238,10 +238,12 @@ struct ConvertOut {
   float* rinv2;                       // [G][MT2 * 128]
 };
 
+// only_heff: convert just the Heff rows (block 0) of GEMM 1, np per set
+// (the driven generator re-splits Heff(t) every step).
 __global__ void convert_kernel(const double2* heff, int64_t heff_stride, const double2* l_ops, int64_t l_stride,
-                               Args a, ConvertOut out) {
+                               Args a, ConvertOut out, int only_heff) {
   const int rows1 = a.MT1 * kBM, rows2 = a.MT2 * kBM;
-  const int per_g = rows1 + (a.K > 0 ? rows2 : 0);
+  const int per_g = only_heff ? a.np : rows1 + (a.K > 0 ? rows2 : 0);
   const int g = blockIdx.x / per_g;
   const int q = blockIdx.x % per_g;
   const int n = a.n, np = a.np;
@@ -266,6 +268,24 @@ __global__ void convert_kernel(const double2* heff, int64_t heff_stride, const d
     const size_t go = (size_t)g * a.MT2 * a.KC2 * kPiece;
     sg::convert_row(elem, y, y < n, a.K * np, a.K * np, a.KC2, out.A2[0] + go, out.A2[1] + go, out.A2[2] + go,
                     out.rinv2 + (size_t)g * rows2);
+  }
+}
+
+// Heff(t) = Heff - sum_q c_q H_q for every generator set (the driven
+// generator, lime/oqs.py:1716-1722), FP64.
+__global__ void heff_t_kernel(const double2* heff, int64_t heff_stride, int G, int n, const double2* ops,
+                              const double* coef, int n_drive, double2* out) {
+  const size_t nn = (size_t)n * n;
+  const size_t total = (size_t)G * nn;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const size_t g = q / nn, e = q % nn;
+    double2 v = heff[(heff_stride ? g * heff_stride : 0) + e];
+    for (int k = 0; k < n_drive; ++k) {
+      const double2 h = ops[(size_t)k * nn + e];
+      v.x -= coef[k] * h.x;
+      v.y -= coef[k] * h.y;
+    }
+    out[q] = v;
   }
 }
 
@@ -605,7 +625,8 @@ int lsm_generators(int P, int64_t heff_stride, int K, int64_t l_stride) {
 
 extern "C" size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops) {
   if (n <= 0 || batch <= 0 || n_generators <= 0 || n_ops < 0) return 0;
-  return lsm_layout(n, batch, n_generators, n_ops).total;
+  // (+ one FP64 Heff(t) per generator set for driven generators)
+  return lsm_layout(n, batch, n_generators, n_ops).total + (size_t)n_generators * n * n * 16;
 }
 
 extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream) {
@@ -620,10 +641,12 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   const int P = d->param_batch > 0 ? d->param_batch : d->batch;
   if (P > d->batch) return LIME_ERR_ARG;
   if (!(d->dt == d->dt)) return LIME_ERR_ARG;
+  if (d->n_drive < 0 || (d->n_drive > 0 && (!d->drive_ops || !d->drive_coef))) return LIME_ERR_ARG;
   const int K = d->n_ops;
   const int G = lsm_generators(P, d->heff_stride, K, d->l_stride);
   const LsmLayout L = lsm_layout(d->n, d->batch, G, K);
-  if (d->workspace_bytes < L.total) return LIME_ERR_WORKSPACE;
+  const size_t drive_bytes = d->n_drive > 0 ? (size_t)G * d->n * d->n * sizeof(double2) : 0;
+  if (d->workspace_bytes < L.total + drive_bytes) return LIME_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
   const int B = d->batch;
   cudaStream_t st = (cudaStream_t)stream;
@@ -664,7 +687,7 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
 
   const int per_g = L.MT1 * 128 + (K > 0 ? L.MT2 * 128 : 0);
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
-                                                  reinterpret_cast<const double2*>(d->l_ops), d->l_stride, a, co);
+                                                  reinterpret_cast<const double2*>(d->l_ops), d->l_stride, a, co, 0);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
   a.B1n[0] = B1[0][0]; a.B1n[1] = B1[0][1];
@@ -681,7 +704,21 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
   const int n_slots = d->n_steps / obs_every;
   int cur = 0;
+  double2* heff_t = reinterpret_cast<double2*>(reinterpret_cast<uint8_t*>(d->workspace) + L.total);
   for (int step = 0; step < d->n_steps; ++step) {
+    if (d->n_drive > 0) {
+      // Heff(t) of this step, re-split into the GEMM 1 pieces
+      const size_t tot = (size_t)G * d->n * d->n;
+      const int hb = (int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535);
+      lsm::heff_t_kernel<<<hb, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride, G, d->n,
+                                             reinterpret_cast<const double2*>(d->drive_ops),
+                                             d->drive_coef + (size_t)step * d->n_drive, d->n_drive, heff_t);
+      LIME_CUDA_TRY(cudaGetLastError());
+      lsm::convert_kernel<<<G * L.np, 256, 0, st>>>(heff_t, G == 1 ? 0 : (int64_t)d->n * d->n, nullptr, 0, a,
+                                                    co, 1);
+      LIME_CUDA_TRY(cudaGetLastError());
+      launches += 2;
+    }
     for (int s = 0; s < 4; ++s) {
       a.rk.stage = s;
       a.B1c[0] = B1[cur][0]; a.B1c[1] = B1[cur][1];
@@ -799,10 +836,10 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
 
   const int per_g = L.MT1 * 128;
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
-                                                  nullptr, 0, af, cf);
+                                                  nullptr, 0, af, cf, 0);
   LIME_CUDA_TRY(cudaGetLastError());
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff_adj),
-                                                  d->heff_adj_stride, nullptr, 0, aa, ca);
+                                                  d->heff_adj_stride, nullptr, 0, aa, ca, 0);
   LIME_CUDA_TRY(cudaGetLastError());
   launches += 2;
   LIME_CUDA_TRY(cudaMemsetAsync(J.Lhi, 0, 2 * L.st, st));   // Lhi and Llo

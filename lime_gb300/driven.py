@@ -21,7 +21,14 @@ from . import engine
 from .result import Result
 
 
-def _lindblad_driven(H, rho0, c_ops=None, e_ops=None, Nt=1, dt=0.005, t0=0., return_result=True):
+def _lindblad_driven(H, rho0, c_ops=None, e_ops=None, Nt=1, dt=0.005, t0=0., return_result=True,
+                     precision='fp64', store_states=True):
+    """``precision='split'`` runs the streaming tensor-core path (Heff(t)
+    re-split on the device every step); it keeps the state on the device, so
+    ``rholist`` then holds the final state only (pass store_states=False)."""
+    if precision == 'split' and return_result and store_states:
+        raise ValueError('precision="split" keeps the state on the device: pass store_states=False '
+                         '(rholist then holds the final state)')
     c_ops = [] if c_ops is None else c_ops
     e_ops = [] if e_ops is None else list(e_ops)
     H0 = H[0]
@@ -42,8 +49,9 @@ def _lindblad_driven(H, rho0, c_ops=None, e_ops=None, Nt=1, dt=0.005, t0=0., ret
     if ops:
         drive = (torch.as_tensor(np.stack(ops), dtype=torch.complex128, device=dev).contiguous(),
                  torch.as_tensor(coef, dtype=torch.float64, device=dev).contiguous())
-    obs, states, rho = engine.propagate(gen, rho0, dt, Nt, e_ops, states_every=1 if return_result else 0,
-                                        drive=drive)
+    obs, states, rho = engine.propagate(gen, rho0, dt, Nt, e_ops,
+                                        states_every=1 if (return_result and store_states) else 0,
+                                        drive=drive, precision=precision)
     if not return_result:
         open('den_mat.dat', 'w').close()
         fmt = '{} ' * (len(e_ops) + 1) + '\n'
@@ -54,5 +62,5 @@ def _lindblad_driven(H, rho0, c_ops=None, e_ops=None, Nt=1, dt=0.005, t0=0., ret
         return rho[0].cpu().numpy()
     res = Result(dt=dt, Nt=Nt, rho0=rho0, t0=t0, nout=1)
     res.observables = obs[0].cpu().numpy()
-    res.rholist = list(states[0].cpu().numpy())
+    res.rholist = list(states[0].cpu().numpy()) if states is not None else [rho[0].cpu().numpy()]
     return res

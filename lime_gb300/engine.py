@@ -307,7 +307,7 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
 
 
 def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
-                obs_every: int, param_batch: int, events=None, max_retries: int = 3):
+                obs_every: int, param_batch: int, events=None, max_retries: int = 3, drive=None):
     """Any generator on the tensor cores (``lime_lindblad_rk4_stream``):
     streaming split-precision GEMMs for Heff rho and sum_k L_k rho L_k^dag.
     State scale: max |rho0| * 1.25 <= 2^13; L_k rho scale from the largest
@@ -362,6 +362,9 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
             d.obs_out = obs_out.data_ptr()
         d.workspace, d.workspace_bytes = aligned, wsb
         d.status = status.data_ptr()
+        if drive is not None:
+            ops, coef = drive
+            d.n_drive, d.drive_ops, d.drive_coef = ops.shape[0], ops.data_ptr(), coef.data_ptr()
         if events is not None:
             events[0].record()
         nat.check(lib.lime_lindblad_rk4_stream(d, _stream_ptr()), 'lime_lindblad_rk4_stream')
@@ -409,19 +412,16 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
         o, s, status = _run_f64(gen, work, dt, n_steps, obs, obs_every, states_every, tol,
                                 param_batch=B, events=events, drive=drive)
     elif precision == 'split':
-        if drive is not None:
-            raise ValueError('precision="split" propagates static generators; use "fp64" for '
-                             'time-dependent Hamiltonians')
         if states_every:
             raise ValueError('precision="split" keeps the state on chip; states_every is not '
                              'supported (use precision="fp64" for rholist output)')
-        if split_supported(gen) is None:
+        if split_supported(gen) is None and drive is None:
             tol = 1e-5 if trace_tol is None else trace_tol
             o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
                                       param_batch=B, events=events)
         else:
             o, s, status, work = _run_stream(gen, work, dt, n_steps, e_ops, obs_every,
-                                             param_batch=B, events=events)
+                                             param_batch=B, events=events, drive=drive)
     else:
         raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
 
@@ -450,7 +450,8 @@ def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     n, n) or None, ``rho`` (B, n, n) final.  ``events``: optional pair of
     CUDA events recorded on the launching stream around the kernel call.
     ``drive``: optional (ops (q, n, n), coef (n_steps, q) float64) device
-    tensors for H(t) = H0 - sum_q coef[k, q] ops[q] during step k (FP64 path).
+    tensors for H(t) = H0 - sum_q coef[k, q] ops[q] during step k (FP64 path,
+    or the streaming tensor-core path with ``precision='split'``).
     """
     return _launch(gen, rho0, dt, n_steps, e_ops, states_every, precision, trace_tol,
                    obs_every, events, drive)(check)

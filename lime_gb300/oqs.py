@@ -205,7 +205,9 @@ class Lindblad_solver:
         if isinstance(self.H, list) and not engine.is_ragged(self.H):
             from .driven import _lindblad_driven
             return _lindblad_driven(self.H, rho0=rho0, c_ops=self.c_ops, e_ops=e_ops,
-                                    Nt=Nt, dt=dt, t0=t0)
+                                    Nt=Nt, dt=dt, t0=t0, return_result=return_result,
+                                    precision=self.precision,
+                                    store_states=store_states if self.precision == 'split' else True)
         return _lindblad(self.H, rho0, c_ops=self.c_ops, e_ops=e_ops, Nt=Nt, dt=dt,
                          return_result=return_result, precision=self.precision, nout=nout,
                          store_states=store_states)
