@@ -61,8 +61,10 @@ struct Args {
 __device__ __forceinline__ size_t inst_floats(const Args& a) { return (size_t)a.W * a.np; }
 
 // f for 8 rows y..y+7 of state column jj of instance b: Z (or 0) + the X
-// terms + the M term, in place.
-__device__ __forceinline__ void assemble_f(const Args& a, int b, int jj, int y, float (&f)[8]) {
+// terms + the M term, in place.  tr: the transposed X run the X terms need,
+// X_c[x][y..y+7] with c = Im for a real column and Re for an imaginary one.
+__device__ __forceinline__ void assemble_f_tr(const Args& a, int b, int jj, int y, const float (&tr)[8],
+                                              float (&f)[8]) {
   const int np = a.np;
   const bool im = jj >= np;
   const int x = im ? jj - np : jj;
@@ -72,12 +74,12 @@ __device__ __forceinline__ void assemble_f(const Args& a, int b, int jj, int y, 
     // Re f = Xi[y][x] + Xi[x][y]
     sg::ld8(X + (size_t)(np + x) * np + y, u);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fadd_rn(u[i], X[(size_t)(np + y + i) * np + x]));
+    for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fadd_rn(u[i], tr[i]));
   } else {
     // Im f = Xr[x][y] - Xr[y][x]
     sg::ld8(X + (size_t)x * np + y, u);
 #pragma unroll
-    for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fsub_rn(X[(size_t)(y + i) * np + x], u[i]));
+    for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fsub_rn(tr[i], u[i]));
   }
   if (a.m != nullptr && x < a.n) {
     const double2* M = a.m + (a.m_stride ? (int64_t)(b % a.P) * a.m_stride : 0);
@@ -95,6 +97,18 @@ __device__ __forceinline__ void assemble_f(const Args& a, int b, int jj, int y, 
       }
     }
   }
+}
+
+// The same with the transposed run read from global memory (strided).
+__device__ __forceinline__ void assemble_f(const Args& a, int b, int jj, int y, float (&f)[8]) {
+  const int np = a.np;
+  const bool im = jj >= np;
+  const int x = im ? jj - np : jj;
+  const float* X = a.Xg + (size_t)b * inst_floats(a) + (size_t)(im ? 0 : np) * np;
+  float tr[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) tr[i] = X[(size_t)(y + i) * np + x];
+  assemble_f_tr(a, b, jj, y, tr, f);
 }
 
 // RK4 stage update of 8 state rows and the next stage input (B1 pieces and,
@@ -205,26 +219,52 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
   sg::teardown(S, a.status);
 }
 
-// The stage update without dense operators (no GEMM 2): one thread per run
-// of 8 rows of one state column.
-__global__ void finish_kernel(Args a, int batch) {
-  const size_t runs = (size_t)a.W * (a.np / 8);
-  const size_t total = (size_t)batch * runs;
-  bool bad = false, range = false;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
-    const int b = (int)(q / runs);
-    const int rem = (int)(q % runs);
-    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
-    float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (a.stage_store != nullptr) {
-      const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
-      float sc[8];
-      sg::ld8(a.Sc + e, sc);
-      sg::st8(a.stage_store + e, sc);
-    }
-    assemble_f(a, b, jj, y, f);
-    update8(a, b, jj, y, f, bad, range);
+// 32 x 32 tiles of the state for the elementwise stage kernels: the
+// transposed X runs come through shared memory (coalesced loads), the rest
+// is read in place.  Block (instance, x tile, y tile); thread -> (component,
+// column x, run of 8 rows).
+struct TileItem {
+  int b, jj, y;
+  float tr[8];
+};
+
+__device__ __forceinline__ TileItem load_tile_item(const Args& a, float (*T)[32][33]) {
+  const int np = a.np, tiles = np / 32;
+  const int b = blockIdx.x / (tiles * tiles);
+  const int t2 = blockIdx.x % (tiles * tiles);
+  const int x0 = (t2 / tiles) * 32, y0 = (t2 % tiles) * 32;
+  const float* X = a.Xg + (size_t)b * inst_floats(a);
+  // T[c][yy][xx] = X_c[x0 + xx][y0 + yy]  (row x0 + xx, column y0 + yy)
+  for (int idx = threadIdx.x; idx < 2 * 32 * 32; idx += blockDim.x) {
+    const int c = idx >> 10, yy = (idx >> 5) & 31, xx = idx & 31;
+    T[c][yy][xx] = X[(size_t)(c * np + y0 + yy) * np + x0 + xx];
   }
+  __syncthreads();
+  const int t = threadIdx.x;
+  const int comp = t >> 7, xl = (t >> 2) & 31, yl = (t & 3) * 8;
+  TileItem it;
+  it.b = b;
+  it.jj = comp * np + x0 + xl;
+  it.y = y0 + yl;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) it.tr[i] = T[comp ? 0 : 1][yl + i][xl];
+  return it;
+}
+
+// The stage update without dense operators (no GEMM 2).
+__global__ void __launch_bounds__(256) finish_kernel(Args a) {
+  __shared__ float T[2][32][33];
+  const TileItem it = load_tile_item(a, T);
+  bool bad = false, range = false;
+  if (a.stage_store != nullptr) {
+    const size_t e = (size_t)it.b * inst_floats(a) + (size_t)it.jj * a.np + it.y;
+    float sc[8];
+    sg::ld8(a.Sc + e, sc);
+    sg::st8(a.stage_store + e, sc);
+  }
+  float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  assemble_f_tr(a, it.b, it.jj, it.y, it.tr, f);
+  update8(a, it.b, it.jj, it.y, f, bad, range);
   if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
   if (range) atomicOr(a.status, LIME_FLAG_RANGE);
 }
@@ -467,52 +507,48 @@ __global__ void adj_start_kernel(Args a, AdjState j, int batch, float dt6) {
 
 // yb_i = L^dag ab_i (Xg = G ab_i from GEMM 1, ab_i in Sc) and the next
 // adjoint stage input (stage i = 4, 3, 2) or the new lam (i = 1).
-__global__ void adj_finish_kernel(Args a, AdjState j, int batch, int stage_i, float c_l, float c_y) {
-  const size_t runs = (size_t)a.W * (a.np / 8);
-  const size_t total = (size_t)batch * runs;
+__global__ void __launch_bounds__(256) adj_finish_kernel(Args a, AdjState j, int stage_i, float c_l, float c_y) {
+  __shared__ float T[2][32][33];
+  const TileItem it = load_tile_item(a, T);
   const float sl = ldexpf(1.f, *j.sl_exp);
   bool range = false;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
-    const int b = (int)(q / runs);
-    const int rem = (int)(q % runs);
-    const int jj = rem / (a.np / 8), y = (rem % (a.np / 8)) * 8;
-    const bool im = jj >= a.np;
-    const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
-    float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    assemble_f(a, b, jj, y, f);
-    float acc[8], hi[8];
-    if (stage_i == 4) {
-      sg::st8(j.LAcc + e, f);
-    } else {
-      sg::ld8(j.LAcc + e, acc);
-      if (stage_i > 1) {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) acc[i] = __fadd_rn(acc[i], f[i]);
-        sg::st8(j.LAcc + e, acc);
-      } else {
-        float lo[8];
-        sg::ld8(j.Lhi + e, hi);
-        sg::ld8(j.Llo + e, lo);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) hi[i] = rk4_final_f32(hi[i], acc[i], f[i], 1.f, 0.f, lo[i]);
-        sg::st8(j.Lhi + e, hi);
-        sg::st8(j.Llo + e, lo);
-      }
-    }
+  const int b = it.b, jj = it.jj, y = it.y;
+  const bool im = jj >= a.np;
+  const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
+  float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  assemble_f_tr(a, b, jj, y, it.tr, f);
+  float acc[8], hi[8];
+  if (stage_i == 4) {
+    sg::st8(j.LAcc + e, f);
+  } else {
+    sg::ld8(j.LAcc + e, acc);
     if (stage_i > 1) {
-      float nx[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) acc[i] = __fadd_rn(acc[i], f[i]);
+      sg::st8(j.LAcc + e, acc);
+    } else {
+      float lo[8];
       sg::ld8(j.Lhi + e, hi);
+      sg::ld8(j.Llo + e, lo);
 #pragma unroll
-      for (int i = 0; i < 8; ++i) nx[i] = __fmaf_rn(c_l, hi[i], __fmul_rn(c_y, f[i]));
-      sg::st8(a.Sn + e, nx);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        nx[i] = __fmul_rn(nx[i], sl);
-        range |= !(fabsf(nx[i]) <= sg::kBMax);
-      }
-      const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
-      sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, im ? jj - a.np : jj, im, nx);
+      for (int i = 0; i < 8; ++i) hi[i] = rk4_final_f32(hi[i], acc[i], f[i], 1.f, 0.f, lo[i]);
+      sg::st8(j.Lhi + e, hi);
+      sg::st8(j.Llo + e, lo);
     }
+  }
+  if (stage_i > 1) {
+    float nx[8];
+    sg::ld8(j.Lhi + e, hi);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) nx[i] = __fmaf_rn(c_l, hi[i], __fmul_rn(c_y, f[i]));
+    sg::st8(a.Sn + e, nx);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      nx[i] = __fmul_rn(nx[i], sl);
+      range |= !(fabsf(nx[i]) <= sg::kBMax);
+    }
+    const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
+    sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, im ? jj - a.np : jj, im, nx);
   }
   if (range) atomicOr(a.status, LIME_FLAG_RANGE);
 }
@@ -532,9 +568,12 @@ __global__ void adj_grad_kernel(Args a, const float* ab, const float* yst, int b
   const int n = a.n, np = a.np;
   const float* A = ab + (size_t)b * inst_floats(a);
   const float* Y = yst + (size_t)b * inst_floats(a);
-  double part[24];
+  // per-thread partial sums in fp32 (a thread sees a few columns; fp64
+  // arithmetic runs at a small fraction of the fp32 rate on this part), the
+  // block reduction in fp64
+  float pf[24];
 #pragma unroll
-  for (int i = 0; i < 24; ++i) part[i] = 0.0;
+  for (int i = 0; i < 24; ++i) pf[i] = 0.f;
   for (int x = threadIdx.x; x < n; x += blockDim.x) {
     float ar[9], ai[9], yr[9], yi[9];
 #pragma unroll
@@ -550,14 +589,17 @@ __global__ void adj_grad_kernel(Args a, const float* ab, const float* yst, int b
     for (int i = 0; i < 8; ++i) {
       const int k = k0 + i;
       if (k < n) {
-        part[i] += 2.0 * ((double)ar[i] * yi[i] - (double)ai[i] * yr[i]);
-        if (x != k) part[16 + i] -= (double)ar[i] * yr[i] + (double)ai[i] * yi[i];
+        pf[i] = __fmaf_rn(2.f, __fmaf_rn(ar[i], yi[i], -ai[i] * yr[i]), pf[i]);
+        if (x != k) pf[16 + i] -= __fmaf_rn(ar[i], yr[i], ai[i] * yi[i]);
         if (k + 1 < n)
-          part[8 + i] += 2.0 * (((double)ar[i] * yi[i + 1] - (double)ai[i] * yr[i + 1]) +
-                                ((double)ar[i + 1] * yi[i] - (double)ai[i + 1] * yr[i]));
+          pf[8 + i] = __fmaf_rn(2.f, __fmaf_rn(ar[i], yi[i + 1], -ai[i] * yr[i + 1]) +
+                                         __fmaf_rn(ar[i + 1], yi[i], -ai[i + 1] * yr[i]), pf[8 + i]);
       }
     }
   }
+  double part[24];
+#pragma unroll
+  for (int i = 0; i < 24; ++i) part[i] = (double)pf[i];
   __shared__ double red[4][24];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
 #pragma unroll
@@ -694,6 +736,7 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   a.Sn = Sbuf[0];
   const size_t runs = (size_t)B * L.W * (L.np / 8);
   const int eb = (int)((runs + 255) / 256 < 65535 ? (runs + 255) / 256 : 65535);
+  const int tb = B * (L.np / 32) * (L.np / 32);            // 32 x 32 state tiles
   lsm::init_kernel<<<eb, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->rho), B);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
@@ -731,7 +774,7 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
       if (K > 0) {
         lsm::gemm_kernel<true><<<B * L.MT2 * L.NT, sg::kThreads, smem, st>>>(a);
       } else {
-        lsm::finish_kernel<<<eb, 256, 0, st>>>(a, B);
+        lsm::finish_kernel<<<tb, 256, 0, st>>>(a);
       }
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
@@ -848,6 +891,7 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
   LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const size_t runs = (size_t)B * L.W * (L.np / 8);
   const int eb = (int)((runs + 255) / 256 < 65535 ? (runs + 255) / 256 : 65535);
+  const int tb = B * (L.np / 32) * (L.np / 32);            // 32 x 32 state tiles
   const int gemm_grid = B * L.MT1 * L.NT;
   const int n_slots = d->n_steps / obs_every;
   const int n_seg = (d->n_steps + seg - 1) / seg;
@@ -874,7 +918,7 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
         af.stage_store = store + ((size_t)s * 4 + k) * B * inst;
         lsm::gemm_kernel<false><<<gemm_grid, sg::kThreads, smem, st>>>(af);
         LIME_CUDA_TRY(cudaGetLastError());
-        lsm::finish_kernel<<<eb, 256, 0, st>>>(af, B);
+        lsm::finish_kernel<<<tb, 256, 0, st>>>(af);
         LIME_CUDA_TRY(cudaGetLastError());
         launches += 2;
         cur ^= 1;
@@ -909,7 +953,7 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
         LIME_CUDA_TRY(cudaGetLastError());
         const float c_l = (float)(i == 2 ? dt / 6.0 : dt / 3.0);
         const float c_y = (float)(i == 4 ? dt : dt / 2.0);
-        lsm::adj_finish_kernel<<<eb, 256, 0, st>>>(aa, J, B, i, c_l, c_y);
+        lsm::adj_finish_kernel<<<tb, 256, 0, st>>>(aa, J, i, c_l, c_y);
         LIME_CUDA_TRY(cudaGetLastError());
         launches += 3;
         if (i > 1) c ^= 1;
