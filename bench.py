@@ -245,16 +245,28 @@ def gpu_arm(args, rank, world, local):
     elif rank == 0:
         fp64 = fp64_leg(gen, rho0, pop_ops, K, obs_every, obs, torch, engine)
     e2e = None
-    if not args.no_e2e and rank == 0:
+    if not args.no_e2e:
+        # every rank runs its shard through the public API; whole-job rate
+        # from the slowest rank
+        if world > 1:
+            torch.distributed.barrier()
         e2e = e2e_leg(wl, K, path, dev)
+        if world > 1:
+            from lime_gb300.replicas import max_over_ranks
+            t_max = max_over_ranks(e2e.pop('wall_s'), device=dev)
+            e2e['value'] = B * world * K / t_max
+        else:
+            e2e.pop('wall_s')
+    # single-GPU legs (other workloads of the path), at N = 1 only
+    single = world == 1
     adj = None
-    if not args.no_adjoint and rank == 0:
+    if not args.no_adjoint and single:
         adj = adjoint_leg(torch, dev, batch=args.adjoint_batch)
     red = None
-    if not args.no_redfield and rank == 0:
+    if not args.no_redfield and single:
         red = redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n, n_rhs=args.redfield_rhs)
     rag = None
-    if not args.no_ragged and rank == 0:
+    if not args.no_ragged and single:
         rag = ragged_leg(torch, dev, batch=args.ragged_batch,
                          sizes=tuple(int(x) for x in args.ragged_sizes.split(',')))
     cpu = None
@@ -537,7 +549,7 @@ def e2e_leg(wl, K, path, dev):
     t = time.perf_counter() - t0
     h2d = H.numel() * 16 + l.numel() * 16 + rho0.size * 16 + N_SITES * N_SITES * 16
     d2h = res.observables.nbytes + np.asarray(res.rholist).nbytes
-    return {'value': B * K / t, 'unit': 'instance-steps/s',
+    return {'value': B * K / t, 'unit': 'instance-steps/s', 'wall_s': t,
             'h2d_bytes_per_step': h2d / K, 'd2h_bytes_per_step': d2h / K,
             'api': 'lime_gb300.oqs.Lindblad_solver.evolve (numpy/pinned host arrays in, '
                    'numpy Result out)'}
