@@ -69,7 +69,7 @@ def _forward_split(gen, work, dt, n_steps, E, obs_every, B, K):
         if engine.split_supported(gen) is None:
             o, _, status = engine._run_split(gen, work, dt, seg, E, obs_every, 1e-5, param_batch=B)
         else:
-            o, _, status, work = engine._run_stream(gen, work, dt, seg, E, obs_every, param_batch=B)
+            o, _, status, work, _ = engine._run_stream(gen, work, dt, seg, E, obs_every, param_batch=B)
         flags = int(status.item())
         if flags:
             raise nat.KernelFlagError(flags, 'chain_observables forward (split)')

@@ -307,13 +307,18 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
 
 
 def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
-                obs_every: int, param_batch: int, events=None, max_retries: int = 3, drive=None):
+                obs_every: int, param_batch: int, events=None, max_retries: int = 3, drive=None,
+                defer: bool = False):
     """Any generator on the tensor cores (``lime_lindblad_rk4_stream``):
     streaming split-precision GEMMs for Heff rho and sum_k L_k rho L_k^dag.
     State scale: max |rho0| * 1.25 <= 2^13; L_k rho scale from the largest
     absolute row sum of the collapse operators; a run whose values leave the
     fixed-point range raises LIME_FLAG_RANGE and is repeated with both
-    scales lowered 4x."""
+    scales lowered 4x.  Returns (obs, None, status, final rho, redo):
+    ``redo()`` relaunches with 4x smaller scales and returns the new
+    (obs, status, rho).  With ``defer=True`` the range check is left to the
+    caller (no host synchronisation after the launch, so launches on other
+    streams are enqueued without waiting); otherwise it is done here."""
     lib = nat.require_device()
     B, n = rho.shape[0], gen.n
     dev = rho.device
@@ -334,8 +339,7 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     lrow = 0.0
     if K:
         lrow = float(gen.l_dense.abs().sum(-1).max().item())
-    sb = _pow2_exponent(8192.0 / 1.25, pmax)
-    sy = _pow2_exponent(8192.0 / 1.25, lrow * pmax) if K else 0
+    scales = [_pow2_exponent(8192.0 / 1.25, pmax), _pow2_exponent(8192.0 / 1.25, lrow * pmax) if K else 0]
     heff_shared = gen.heff.shape[0] == 1
     l_shared = gen.l_dense is None or gen.l_dense.shape[0] == 1
     G = 1 if (heff_shared and l_shared) else param_batch
@@ -343,13 +347,14 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
     aligned = (ws.data_ptr() + 1023) // 1024 * 1024
     start = rho.contiguous()
-    for attempt in range(max_retries + 1):
+
+    def launch():
         work = start.clone()
         status.zero_()
         d = nat.LindbladStreamDesc()
         d.n, d.batch, d.param_batch, d.n_ops = n, B, param_batch, K
         d.n_steps, d.n_obs, d.obs_every = n_steps, n_obs, obs_every
-        d.scale_b_log2, d.scale_y_log2 = max(-60, min(60, sb)), max(-60, min(60, sy))
+        d.scale_b_log2, d.scale_y_log2 = max(-60, min(60, scales[0])), max(-60, min(60, scales[1]))
         d.dt = float(dt)
         d.rho = work.data_ptr()
         d.heff, d.heff_stride = gen.heff.data_ptr(), (0 if heff_shared else n * n)
@@ -370,20 +375,29 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
         nat.check(lib.lime_lindblad_rk4_stream(d, _stream_ptr()), 'lime_lindblad_rk4_stream')
         if events is not None:
             events[1].record()
-        if attempt < max_retries and int(status.item()) & nat.LIME_FLAG_RANGE:
-            sb -= 2
-            sy -= 2
-            continue
-        break
-    return obs_out[:, :n_slots, :n_obs], None, status, work
+        return work
+
+    def redo():
+        scales[0] -= 2
+        scales[1] -= 2
+        return obs_out[:, :n_slots, :n_obs], status, launch()
+
+    work = launch()
+    if not defer:
+        for _ in range(max_retries):
+            if not int(status.item()) & nat.LIME_FLAG_RANGE:
+                break
+            _, _, work = redo()
+    return obs_out[:, :n_slots, :n_obs], None, status, work, redo
 
 
 def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
-            obs_every: int = 1, events=None, drive=None):
+            obs_every: int = 1, events=None, drive=None, defer: bool = False):
     """Enqueue one propagation on the current stream; returns a closure that
     checks the status word (synchronising the stream) and assembles
-    ``(obs, states, rho)``."""
+    ``(obs, states, rho)``.  ``defer``: nothing after the launch waits for
+    the GPU (range retries of the streaming path happen in the closure)."""
     if obs_every < 1 or states_every < 0 or n_steps < 0:
         raise ValueError('obs_every must be >= 1, states_every >= 0, n_steps >= 0')
     device = gen.heff.device
@@ -407,6 +421,7 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     else:
         a, b = hermitian_parts(rho)
         work = torch.cat([a, b], 0).contiguous()
+    redo = None
     if precision == 'fp64':
         tol = 1e-9 if trace_tol is None else trace_tol
         o, s, status = _run_f64(gen, work, dt, n_steps, obs, obs_every, states_every, tol,
@@ -420,12 +435,19 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
                                       param_batch=B, events=events)
         else:
-            o, s, status, work = _run_stream(gen, work, dt, n_steps, e_ops, obs_every,
-                                             param_batch=B, events=events, drive=drive)
+            o, s, status, work, redo = _run_stream(gen, work, dt, n_steps, e_ops, obs_every,
+                                                   param_batch=B, events=events, drive=drive,
+                                                   defer=defer)
     else:
         raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
 
     def finish(check: bool = True):
+        nonlocal o, status, work
+        if redo is not None:
+            for _ in range(3):
+                if not int(status.item()) & nat.LIME_FLAG_RANGE:
+                    break
+                o, status, work = redo()
         if check:
             flags = int(status.item())
             if flags:
@@ -515,7 +537,7 @@ def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None
             E = [torch.stack([as_device(e_ops_list[i][o], device) for i in idx])
                  for o in range(len(e_ops_list[idx[0]]))]
             fin = _launch(gen, rho, dt, n_steps, E, states_every=states_every, precision=precision,
-                          trace_tol=trace_tol, obs_every=obs_every)
+                          trace_tol=trace_tol, obs_every=obs_every, defer=True)
         pending.append((idx, st, fin))
     obs, states, rhos = [None] * B, [None] * B, [None] * B
     for idx, st, fin in pending:
