@@ -137,3 +137,29 @@ def test_multi_operator_correlations_split():
     assert rel(sol.correlation_4op_1t(rho0, ops, dt, 30), g['c4op_1t']) < TOL
     assert rel(sol.correlation_3op_2t(rho0, ops[:3], dt, 12, 10), g['c3op_2t']) < TOL
     assert rel(sol.correlation_4op_2t(rho0, ops, dt, 12, 10), g['c4op_2t']) < TOL
+
+
+@pytest.mark.parametrize('n', [1, 2, 3])
+def test_tiny_dimensions(n):
+    from lime_gb300 import engine
+    rng = np.random.default_rng(60 + n)
+    if n == 1:
+        H, c_ops = np.array([[0.3]], dtype=complex), [np.array([[0.1 + 0.05j]])]
+    else:
+        H, c_ops = chains.uneven_chain(n, rng, n_ops=2)
+    gen = engine.LindbladGenerator.build(H, c_ops)
+    (o64, r64), (osp, rsp) = _both(gen, chains.ground_dm(n), 40, [chains.population_ops(n)[0]])
+    assert _dev(osp, o64) < TOL
+    assert _dev(rsp, r64) < TOL
+
+
+def test_zero_steps_returns_the_input():
+    from lime_gb300 import engine
+    rng = np.random.default_rng(70)
+    H, c_ops = chains.uneven_chain(10, rng, n_ops=2)
+    gen = engine.LindbladGenerator.build(H, c_ops)
+    psi = rng.normal(size=10) + 1j * rng.normal(size=10)
+    rho0 = np.outer(psi, psi.conj()) / np.vdot(psi, psi).real
+    obs, _, rho = engine.propagate(gen, rho0, 0.05, 0, [chains.population_ops(10)[0]], precision='split')
+    assert obs.shape == (1, 0, 1)
+    assert _dev(rho[0].cpu().numpy(), rho0) < 1e-7          # fp32 hi + lo round trip
