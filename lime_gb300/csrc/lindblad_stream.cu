@@ -161,8 +161,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
       // ---- X rows (block 0): the tile columns into Xg, runs of 8 rows
       const int nlo = lane & 7, glo = lane >> 3;
 #pragma unroll 1
-      for (int it = 0; it < 8; ++it) {
-        const int wi = it * 8 + ew;
+      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
         const int jl = (wi >> 2) * 8 + nlo;
         const int dl = ((wi & 3) * 4 + glo) * 8;
         const int R = mt * kBM + dl;
@@ -174,14 +173,15 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
       }
       // ---- Y_k rows (blocks 1..K): Y^dag into B2, runs of 8 columns of one row
       const int r = u & 127, o0 = u >> 7;
+      constexpr int kGroups = sg::kEpiThreads / 128;
       const int R = mt * kBM + r;
       const int blk = R / np, yrow = R - blk * np;
       if (blk >= 1 && blk <= a.K) {
         uint8_t* B20 = a.B2[0] + (size_t)b * a.NT * a.KC2 * kPiece;
         uint8_t* B21 = a.B2[1] + (size_t)b * a.NT * a.KC2 * kPiece;
 #pragma unroll 1
-        for (int i = 0; i < 8; ++i) {
-          const int cl = 8 * (o0 + 2 * i);
+        for (int i = 0; i < 16 / kGroups; ++i) {
+          const int cl = 8 * (o0 + kGroups * i);
           const int jj = nt * kBN + cl;
           const bool im = jj >= np;
           const int x = im ? jj - np : jj;
@@ -200,8 +200,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
       // ---- f = Z + X terms + M term and the RK4 stage update, runs of 8 rows
       const int nlo = lane & 7, glo = lane >> 3;
 #pragma unroll 1
-      for (int it = 0; it < 8; ++it) {
-        const int wi = it * 8 + ew;
+      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
         const int jl = (wi >> 2) * 8 + nlo;
         const int dl = ((wi & 3) * 4 + glo) * 8;
         const int y = mt * kBM + dl, jj = nt * kBN + jl;

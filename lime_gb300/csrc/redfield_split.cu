@@ -75,17 +75,17 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
   if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
     const int u = t - sg::kEpiFirst, ew = u >> 5;
     if (kObserve) {
-      // row r = observable, 64 columns of one half per thread
+      // row r = observable, kEpiCols columns per thread
       const int r = u & 127, hh = u >> 7;
       const int o = mt * kBM + r;
       if (o < a.n_obs && KC > 0) {
 #pragma unroll 4
-        for (int c = 0; c < 64; ++c) {
-          const int jj = nt * kBN + 64 * hh + c;
+        for (int c = 0; c < sg::kEpiCols; ++c) {
+          const int jj = nt * kBN + sg::kEpiCols * hh + c;
           const int j = jj < a.Rp ? jj : jj - a.Rp;
           if (j < a.R)
             atomicAdd(a.obs + 2 * ((size_t)j * a.n_obs + o) + (jj < a.Rp ? 0 : 1),
-                      (double)ft[(64 * hh + c) * kFStride + r]);
+                      (double)ft[(sg::kEpiCols * hh + c) * kFStride + r]);
         }
       }
     } else {
@@ -94,8 +94,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
       const sg::RK4 k4{a.stage, a.c_half, a.c_full, a.c_sixth, a.c_sixth_lo};
       bool bad = false, range = false;
 #pragma unroll 1
-      for (int it = 0; it < 8; ++it) {
-        const int wi = it * 8 + ew;
+      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
         const int jl = (wi >> 2) * 8 + nlo;
         const int dl = ((wi & 3) * 4 + glo) * 8;
         const int jj = nt * kBN + jl, d = mt * kBM + dl;
