@@ -39,6 +39,12 @@
 // each thread write its own row segment of the next B operand
 // (B^T row i = [Re rho[i][:], -Im rho[i][:]]).  Observables, the trace check
 // and the final state are produced in FP64 from hi + lo.
+//
+// Units.  Each thread keeps its state component already in B units
+// (R = +-2^b rho, the sign of the B^T row it writes) and its RK4 sums in
+// accumulator units (X = 2^(a+b) Heff rho): the conversion factors are powers
+// of two folded into dt/2, dt and dt/6, so the epilogue multiplies by no scale
+// and the results are those of the natural-unit arithmetic scaled exactly.
 
 #include "common.cuh"
 #include "tc_ptx.cuh"
@@ -70,7 +76,9 @@ struct __align__(1024) Smem {
 
 struct Args {
   int n, batch, param_batch, n_steps, step0, obs_mode, n_obs, obs_every, obs_per_inst;
-  float sb, inv_sab, sab_half, c_half, c_full, c_sixth, c_sixth_lo;
+  // sb = 2^b, inv_sb = 2^-b, sa_half = 2^(a-1); the RK4 constants dt/2, dt,
+  // dt/6 (+ its low part) multiplied by 2^-a (accumulator -> B units)
+  float sb, inv_sb, sa_half, c_half, c_full, c_sixth, c_sixth_lo;
   double sa_d;
   double trace_tol;
   double2* rho;
@@ -145,20 +153,27 @@ __device__ __forceinline__ void store_b8(Smem& S, uint32_t off, const float* x, 
   *reinterpret_cast<uint4*>(S.bop[1] + off) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
 }
 
-// Issue one MMA pass on thread 0 and wait for it; returns false on timeout.
+// Issue one MMA pass (thread 0) and commit it to mbar; every thread then
+// waits on mbar itself (bounded), and the next __syncthreads_or turns any
+// thread's timeout into a common abort.  No thread can fall two phases
+// behind: each pass is issued only after a barrier that every thread reaches
+// after its wait on the previous one.  desc_b0 / desc_b1: descriptors of K
+// step 0; K step ks starts 2 * kLBO * ks bytes further, i.e.
+// (2 * kLBO / 16) * ks in the descriptor's address field (the operands lie
+// far below the field's 256 KB limit, so no carry).
 template <bool kExact>
-__device__ __forceinline__ bool mma_pass(uint32_t tbase, uint32_t b0_addr, uint32_t b1_addr, uint64_t* mbar,
-                                         uint32_t parity, uint32_t max_wait) {
+__device__ __forceinline__ void mma_pass(uint32_t tbase, uint64_t desc_b0, uint64_t desc_b1, uint64_t* mbar) {
   constexpr uint32_t idesc = tc::idesc_f16(128, 64, 0);
+  constexpr uint64_t kDescStep = 2 * kLBO / 16;
   tc::tc_fence_after();
 #pragma unroll
   for (int ks = 0; ks < 8; ++ks) {
-    const uint64_t d0 = tc::smem_desc_noswizzle(b0_addr + ks * 2 * kLBO, kLBO, kSBO);
+    const uint64_t d0 = desc_b0 + kDescStep * ks;
     const uint32_t acc = ks > 0 ? 1u : 0u;
     if (kExact) {
       tc::mma_f16_ts(tbase + kColD, tbase + kColA0 + ks * 8, d0, idesc, acc);
     } else {
-      const uint64_t d1 = tc::smem_desc_noswizzle(b1_addr + ks * 2 * kLBO, kLBO, kSBO);
+      const uint64_t d1 = desc_b1 + kDescStep * ks;
       tc::mma_f16_ts(tbase + kColD, tbase + kColA1 + ks * 8, d0, idesc, acc);
       tc::mma_f16_ts(tbase + kColD, tbase + kColA0 + ks * 8, d1, idesc, 1u);
       tc::mma_f16_ts(tbase + kColD, tbase + kColA1 + ks * 8, d1, idesc, 1u);
@@ -166,7 +181,6 @@ __device__ __forceinline__ bool mma_pass(uint32_t tbase, uint32_t b0_addr, uint3
     }
   }
   tc::mma_commit(mbar);
-  return tc::mbar_wait_bounded(mbar, parity, max_wait);
 }
 
 __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a) {
@@ -195,11 +209,12 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
   tc::tc_fence_after();
   const uint32_t tbase = S.tmem_base;
   const uint32_t lane_addr = tbase + ((uint32_t)(lq * 32) << 16);
-  const uint32_t b0_addr = tc::smem_u32(S.bop[0]);
-  const uint32_t b1_addr = tc::smem_u32(S.bop[1]);
+  const uint64_t desc_b0 = tc::smem_desc_noswizzle(tc::smem_u32(S.bop[0]), kLBO, kSBO);
+  const uint64_t desc_b1 = tc::smem_desc_noswizzle(tc::smem_u32(S.bop[1]), kLBO, kSBO);
   const uint32_t brow = (uint32_t)(i >> 3) * kSBO + (uint32_t)(i & 7) * 16u;
   const uint32_t bchunk0 = (is_re ? 0u : 8u) + 4u * (uint32_t)h;
-  const float bsign = is_re ? a.sb : -a.sb;
+  const float bsign = is_re ? a.sb : -a.sb;   // natural -> B units of this thread's component
+  const float tsign = is_re ? 1.f : -1.f;      // u = own +- transposed element
   float* xrow = S.xt + r * kXtStride;
   const float* xcol = S.xt + (is_re ? 64 : 0) * kXtStride + i;   // X[j][i] at xcol[j * stride]
   uint32_t phase = 0;
@@ -243,7 +258,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       tc::tmem_wait_st();
     }
 
-    // ---- state: columns [j0, j0+32) of this thread's row component ----
+    // ---- state: columns [j0, j0+32) of this thread's row component, B units ----
     float rho[kCols], acc[kCols];
     const double2* r0 = a.rho + (int64_t)b * n * n;
     double dtr = 0.0;
@@ -258,10 +273,11 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         v = is_re ? z.x : z.y;
       }
       const float hv = (float)v;
-      rho[jj] = hv;
-      S.rlo[j * 128 + r] = (float)(v - (double)hv);
-      mx = fmaxf(mx, fabsf(hv * a.sb));
-      if (diag_owner && j == i) { dtr = v; rho_d = hv; }
+      rho[jj] = hv * bsign;
+      acc[jj] = 0.f;
+      S.rlo[j * 128 + r] = (float)(v - (double)hv) * bsign;
+      mx = fmaxf(mx, fabsf(rho[jj]));
+      if (diag_owner && j == i) { dtr = v; rho_d = rho[jj]; }
     }
     rs_d = rho_d;
     S.smax[g & 1][t] = mx;
@@ -275,7 +291,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       for (int c = 0; c < 4; ++c) {
         float x[8];
 #pragma unroll
-        for (int e = 0; e < 8; ++e) x[e] = rho[8 * c + e] * bsign;
+        for (int e = 0; e < 8; ++e) x[e] = rho[8 * c + e];
         store_b8(S, brow + (bchunk0 + c) * kLBO, x, magic, dummy);
       }
     }
@@ -288,106 +304,108 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         tc::fence_proxy_async_smem();
         tc::tc_fence_before();
         __syncthreads();
-        int timed_out = 0;
-        if (t == 0) timed_out = mma_pass<false>(tbase, b0_addr, b1_addr, &S.mbar, phase, a.max_wait) ? 0 : 1;
+        if (t == 0) mma_pass<false>(tbase, desc_b0, desc_b1, &S.mbar);
+        int timed_out = tc::mbar_wait_bounded(&S.mbar, phase, a.max_wait) ? 0 : 1;
         phase ^= 1u;
-        if (__syncthreads_or(timed_out)) {
-          aborted = true;
-          break;
-        }
         tc::tc_fence_after();
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          float v[16];
-          tc::tmem_ld16(lane_addr + kColD + j0 + q * 16, v);
-#pragma unroll
-          for (int e = 0; e < 4; ++e)
-            *reinterpret_cast<float4*>(xrow + j0 + q * 16 + 4 * e) =
-                make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
-        }
+        float v1[32];   // held in registers across pass 2
+        tc::tmem_ld32(lane_addr + kColD + j0, v1);
         // ---- pass 2: the exact product A0.B0 into D ----
         tc::tc_fence_before();
-        __syncthreads();
-        if (t == 0) timed_out = mma_pass<true>(tbase, b0_addr, b1_addr, &S.mbar, phase, a.max_wait) ? 0 : 1;
-        phase ^= 1u;
         if (__syncthreads_or(timed_out)) {
           aborted = true;
           break;
         }
+        if (t == 0) mma_pass<true>(tbase, desc_b0, desc_b1, &S.mbar);
+        timed_out = tc::mbar_wait_bounded(&S.mbar, phase, a.max_wait) ? 0 : 1;
+        phase ^= 1u;
         tc::tc_fence_after();
+        {
+          float v[32];
+          tc::tmem_ld32(lane_addr + kColD + j0, v);
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          float v[16];
-          tc::tmem_ld16(lane_addr + kColD + j0 + q * 16, v);
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            float4* p4 = reinterpret_cast<float4*>(xrow + j0 + q * 16 + 4 * e);
-            const float4 o = *p4;
-            *p4 = make_float4(__fadd_rn(v[4 * e], o.x), __fadd_rn(v[4 * e + 1], o.y),
-                              __fadd_rn(v[4 * e + 2], o.z), __fadd_rn(v[4 * e + 3], o.w));
-          }
+          for (int e = 0; e < 8; ++e)
+            *reinterpret_cast<float4*>(xrow + j0 + 4 * e) =
+                make_float4(__fadd_rn(v[4 * e], v1[4 * e]), __fadd_rn(v[4 * e + 1], v1[4 * e + 1]),
+                            __fadd_rn(v[4 * e + 2], v1[4 * e + 2]), __fadd_rn(v[4 * e + 3], v1[4 * e + 3]));
         }
         // dephasing jump term m_i rho_ii folded into the diagonal of X (it
-        // enters Re f_ii = (X_ii + X_ii) / (sa sb) twice, hence the half)
-        if (diag_owner) xrow[i] = __fmaf_rn(mi * a.sab_half, rs_d, xrow[i]);
+        // enters Re f_ii = X_ii + X_ii twice, hence the half; rs_d is in B units)
+        if (diag_owner) xrow[i] = __fmaf_rn(mi * a.sa_half, rs_d, xrow[i]);
         const float m4 = fmaxf(fmaxf(S.smax[g & 1][i], S.smax[g & 1][64 + i]),
                                fmaxf(S.smax[g & 1][128 + i], S.smax[g & 1][192 + i]));
         const float magic = row_magic(m4);
-        __syncthreads();
-
-        const float cst = (s == 2) ? a.c_full : a.c_half;
-        float nmx = 0.f;
-        // diagonal element, with exactly the operations the loop applies to it
-        float rs_d_next = rs_d;
-        float lo_d = 0.f;
-        if (diag_owner) {
-          const float xd = xrow[i];
-          const float fd = __fmul_rn(__fadd_rn(xd, xd), a.inv_sab);
-          if (s == 0) acc_d = fd;
-          else if (s < 3) acc_d = __fmaf_rn(2.f, fd, acc_d);
-          if (s < 3) {
-            rs_d_next = __fmaf_rn(cst, fd, rho_d);
-          } else {
-            lo_d = S.rlo[i * 128 + r];
-            rho_d = rk4_final_f32(rho_d, acc_d, fd, a.c_sixth, a.c_sixth_lo, lo_d);
-            rs_d_next = rho_d;
-          }
+        if (__syncthreads_or(timed_out)) {
+          aborted = true;
+          break;
         }
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-          float own[16];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float4 o = *reinterpret_cast<const float4*>(xrow + j0 + q * 16 + 4 * e);
-            own[4 * e] = o.x; own[4 * e + 1] = o.y; own[4 * e + 2] = o.z; own[4 * e + 3] = o.w;
+
+        // RK4 in accumulator units: u = 2^(a+b) (+-f), acc += w u, next stage
+        // input R + c u (c = dt/2 or dt in B units); the last stage combines
+        // R + (acc + u) dt/6 on the (hi, lo) pair and clears acc.
+        float nmx = 0.f;
+        if (s < 3) {
+          const float cst = (s == 2) ? a.c_full : a.c_half;
+          const float wgt = (s == 0) ? 1.f : 2.f;
+          float rs_d_next = rs_d;
+          if (diag_owner) {
+            const float xd = xrow[i];
+            const float ud = __fadd_rn(xd, xd);
+            acc_d = __fmaf_rn(wgt, ud, acc_d);
+            rs_d_next = __fmaf_rn(cst, ud, rho_d);
           }
-          float nxt[16];
 #pragma unroll
-          for (int e = 0; e < 16; ++e) {
-            const int jj = q * 16 + e;
-            const float tr = xcol[(j0 + jj) * kXtStride];
-            const float f = __fmul_rn(is_re ? __fadd_rn(own[e], tr) : __fsub_rn(tr, own[e]), a.inv_sab);
-            if (s == 0) acc[jj] = f;
-            else if (s < 3) acc[jj] = __fmaf_rn(2.f, f, acc[jj]);
-            if (s < 3) {
-              nxt[e] = __fmaf_rn(cst, f, rho[jj]);
-            } else {
-              float lo = S.rlo[(j0 + jj) * 128 + r];
-              rho[jj] = rk4_final_f32(rho[jj], acc[jj], f, a.c_sixth, a.c_sixth_lo, lo);
-              S.rlo[(j0 + jj) * 128 + r] = lo;
-              nxt[e] = rho[jj];
+          for (int q = 0; q < 2; ++q) {
+            float own[16];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float4 o = *reinterpret_cast<const float4*>(xrow + j0 + q * 16 + 4 * e);
+              own[4 * e] = o.x; own[4 * e + 1] = o.y; own[4 * e + 2] = o.z; own[4 * e + 3] = o.w;
             }
+            float nxt[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+              const int jj = q * 16 + e;
+              const float u = __fmaf_rn(tsign, xcol[(j0 + jj) * kXtStride], own[e]);
+              acc[jj] = __fmaf_rn(wgt, u, acc[jj]);
+              nxt[e] = __fmaf_rn(cst, u, rho[jj]);
+            }
+#pragma unroll
+            for (int h8 = 0; h8 < 2; ++h8)
+              store_b8(S, brow + (bchunk0 + 2 * q + h8) * kLBO, nxt + 8 * h8, magic, nmx);
+          }
+          rs_d = rs_d_next;
+        } else {
+          if (diag_owner) {
+            const float xd = xrow[i];
+            float lo_d = S.rlo[i * 128 + r];
+            rho_d = rk4_final_f32(rho_d, acc_d, __fadd_rn(xd, xd), a.c_sixth, a.c_sixth_lo, lo_d);
+            acc_d = 0.f;
+            rs_d = rho_d;
           }
 #pragma unroll
-          for (int h8 = 0; h8 < 2; ++h8) {
-            float x[8];
+          for (int q = 0; q < 2; ++q) {
+            float own[16];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) x[e] = nxt[8 * h8 + e] * bsign;
-            store_b8(S, brow + (bchunk0 + 2 * q + h8) * kLBO, x, magic, nmx);
+            for (int e = 0; e < 4; ++e) {
+              const float4 o = *reinterpret_cast<const float4*>(xrow + j0 + q * 16 + 4 * e);
+              own[4 * e] = o.x; own[4 * e + 1] = o.y; own[4 * e + 2] = o.z; own[4 * e + 3] = o.w;
+            }
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+              const int jj = q * 16 + e;
+              const float u = __fmaf_rn(tsign, xcol[(j0 + jj) * kXtStride], own[e]);
+              float lo = S.rlo[(j0 + jj) * 128 + r];
+              rho[jj] = rk4_final_f32(rho[jj], acc[jj], u, a.c_sixth, a.c_sixth_lo, lo);
+              S.rlo[(j0 + jj) * 128 + r] = lo;
+              acc[jj] = 0.f;
+            }
+#pragma unroll
+            for (int h8 = 0; h8 < 2; ++h8)
+              store_b8(S, brow + (bchunk0 + 2 * q + h8) * kLBO, rho + q * 16 + 8 * h8, magic, nmx);
           }
         }
         S.smax[(g + 1) & 1][t] = nmx;
-        rs_d = rs_d_next;
       }
       if (aborted) break;
 
@@ -396,7 +414,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       if (((gstep + 1) % a.obs_every) == 0) {
         const int slot = (gstep + 1) / a.obs_every - 1;
         double2* orow = a.obs_out + ((int64_t)b * a.obs_per_inst + slot) * a.n_obs;
-        const double dval = diag_owner ? (double)rho_d + (double)S.rlo[i * 128 + r] : 0.0;
+        const double dval = diag_owner ? ((double)rho_d + (double)S.rlo[i * 128 + r]) * (double)a.inv_sb : 0.0;
         if (a.obs_mode == 1) {
           if (diag_owner && i < a.n_obs) orow[i] = make_double2(dval, 0.0);
         } else if (a.obs_mode == 2) {
@@ -411,18 +429,19 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
                 if (j < n) {
                   const double2 ev = E[(int64_t)j * n + i];   // E[j][i]
                   const float er = (float)ev.x, ei = (float)ev.y;
+                  // B units: rho[jj] = 2^b Re rho_ij, or -2^b Im rho_ij
                   if (is_re) {
                     pr = __fmaf_rn(er, rho[jj], pr);
                     pi = __fmaf_rn(ei, rho[jj], pi);
                   } else {
-                    pr = __fmaf_rn(-ei, rho[jj], pr);
-                    pi = __fmaf_rn(er, rho[jj], pi);
+                    pr = __fmaf_rn(ei, rho[jj], pr);
+                    pi = __fmaf_rn(-er, rho[jj], pi);
                   }
                 }
               }
             }
-            const double sr = block_sum((double)pr, S.red[0], t);
-            const double si = block_sum((double)pi, S.red[1], t);
+            const double sr = block_sum((double)pr, S.red[0], t) * (double)a.inv_sb;
+            const double si = block_sum((double)pi, S.red[1], t) * (double)a.inv_sb;
             if (t == 0) orow[o] = make_double2(sr, si);
           }
         }
@@ -437,11 +456,12 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
     // ---- final state: rho = hi + lo in FP64 ----
     if (i < n) {
       double* out = reinterpret_cast<double*>(a.rho + (int64_t)b * n * n);
+      const double to_nat = is_re ? (double)a.inv_sb : -(double)a.inv_sb;
 #pragma unroll
       for (int jj = 0; jj < kCols; ++jj) {
         const int j = j0 + jj;
         if (j < n) {
-          const double v = (double)rho[jj] + (double)S.rlo[j * 128 + r];
+          const double v = ((double)rho[jj] + (double)S.rlo[j * 128 + r]) * to_nat;
           if (!isfinite(v)) flags |= LIME_FLAG_NONFINITE;
           out[2 * ((int64_t)i * n + j) + (is_re ? 0 : 1)] = v;
         }
@@ -500,12 +520,17 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   a.obs_per_inst = d->n_steps / a.obs_every;
   a.sa_d = ldexp(1.0, d->scale_a_log2);
   a.sb = ldexpf(1.f, d->scale_b_log2);
-  a.inv_sab = ldexpf(1.f, -(d->scale_a_log2 + d->scale_b_log2));
-  a.sab_half = ldexpf(1.f, d->scale_a_log2 + d->scale_b_log2 - 1);
-  a.c_half = (float)(d->dt / 2.0);
-  a.c_full = (float)d->dt;
-  a.c_sixth = (float)(d->dt / 6.0);
-  a.c_sixth_lo = (float)(d->dt / 6.0 - (double)a.c_sixth);
+  a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
+  a.sa_half = ldexpf(1.f, d->scale_a_log2 - 1);
+  {
+    // the fp32 constants of the natural-unit update, then scaled by 2^-a (exact)
+    const float c6 = (float)(d->dt / 6.0);
+    const float c6lo = (float)(d->dt / 6.0 - (double)c6);
+    a.c_half = ldexpf((float)(d->dt / 2.0), -d->scale_a_log2);
+    a.c_full = ldexpf((float)d->dt, -d->scale_a_log2);
+    a.c_sixth = ldexpf(c6, -d->scale_a_log2);
+    a.c_sixth_lo = ldexpf(c6lo, -d->scale_a_log2);
+  }
   a.trace_tol = d->trace_tol;
   a.rho = reinterpret_cast<double2*>(d->rho);
   a.heff = reinterpret_cast<const double2*>(d->heff); a.heff_stride = d->heff_stride;
