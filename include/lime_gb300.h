@@ -414,6 +414,27 @@ typedef struct {
 int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream);
 
 /* ------------------------------------------------------------------ */
+/* Self-test of the bounded device-side waits (test infrastructure)     */
+/* ------------------------------------------------------------------ */
+/* Every device-side wait of the entry points above polls an mbarrier at most
+ * a bounded number of times; on expiry the kernel ORs LIME_FLAG_TIMEOUT
+ * into its status word, releases its tensor memory and returns (the C
+ * ABI's "wait timeout" status; the context stays usable).  This entry point
+ * makes such waits expire on purpose, with max_wait polls:
+ *   kind 0  one CTA waits on an mbarrier that nothing completes  -> TIMEOUT
+ *   kind 1  the same barrier, completed first (control)          -> 0
+ *   kind 2  the streaming split-precision GEMM tile of the Redfield and
+ *           general Lindblad paths with its operand copies withheld: the
+ *           MMA and epilogue waits expire, the tile aborts      -> TIMEOUT
+ *   kind 3  the same tile with its copies issued (control)       -> 0
+ * ws (kinds 2, 3; 16-byte aligned): lime_wait_selftest_workspace() bytes =
+ * 10 zero operand pieces of 16 KB followed by 128 float row scales (1.0);
+ * the control checks that the tile of zero operands comes out zero
+ * (LIME_FLAG_NONFINITE otherwise).  status: device int32. */
+size_t lime_wait_selftest_workspace(void);
+int lime_wait_selftest(int kind, uint32_t max_wait, const void* ws, int32_t* status, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* Library info                                                         */
 /* ------------------------------------------------------------------ */
 

@@ -185,6 +185,8 @@ SIGNATURES = [
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),
+    ('lime_wait_selftest_workspace', c_size_t, []),
+    ('lime_wait_selftest', c_int32, [c_int32, ctypes.c_uint32, c_void_p, c_void_p, c_void_p]),
     ('lime_device_check', c_int32, []),
     ('lime_launch_count', c_int64, []),
     ('lime_status_string', ctypes.c_char_p, [c_int32]),

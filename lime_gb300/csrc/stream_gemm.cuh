@@ -183,6 +183,7 @@ struct Tile {
   const float* row_inv;    // 128 per-row inverse A scales of the tile (0 on padding rows)
   float inv_sb;            // inverse B scale
   uint32_t max_wait;       // bound on every mbarrier poll loop
+  int withhold = 0;        // self-test only: the producer issues no copies, so every wait expires
 };
 
 // TMEM allocation and barrier set-up; every thread of the CTA calls it.
@@ -239,7 +240,7 @@ __device__ __forceinline__ bool mainloop(Smem& S, const Tile& T) {
         const int s = c % kStages;
         const uint32_t ph = (uint32_t)(c / kStages) & 1u;
         if (!tc::mbar_wait_bounded(&S.empty[s], ph ^ 1u, T.max_wait)) { atomicExch(&S.abort, 1); break; }
-        if (*(volatile int*)&S.abort) break;
+        if (*(volatile int*)&S.abort || T.withhold) break;
         issued = c + 1;
         tc::mbar_arrive_expect_tx(&S.full[s], 5 * kPiece);
         const size_t off = (size_t)(T.c0 + c) * kPiece;
