@@ -477,8 +477,9 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
                err_steps=200):
     """Uneven batch: 1024 chains with N uniform over {8..256}, three dense
     complex collapse operators each (2000-step workload; samples of steps
-    are timed).  Like ``engine.propagate_ragged``: one batched launch
-    sequence per size, the sizes on concurrent streams.  The generators are
+    are timed).  The groups of ``engine.propagate_ragged`` (one batched
+    launch sequence per size, chains of N <= 32 packed block-diagonally on
+    the split path), the sizes on concurrent streams.  The generators are
     prepared once; CUDA events on the joining stream time the GPU work of a
     whole call (all sizes), and the split per-step time is the difference of
     a 20- and a 40-step call (the per-call operand conversion cancels).  The
@@ -489,33 +490,29 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
     w = chains.uneven_batch(batch=batch, sizes=sizes, n_steps=steps_split)
     ns = w['ns']
     E = [[chains.population_ops(int(n))[0]] for n in ns]
-    groups = {}
-    for i, n in enumerate(ns):
-        groups.setdefault(int(n), []).append(i)
     main = torch.cuda.current_stream(dev)
-    prepared = []
-    for n, idx in sorted(groups.items()):
-        H = torch.stack([engine.as_device(w['H'][i], dev) for i in idx])
-        ops = [torch.stack([engine.as_device(w['c_ops'][i][k], dev) for i in idx]) for k in range(3)]
-        gen = engine.LindbladGenerator.build(H, ops, device=dev)
-        rho = torch.stack([engine.as_device(w['rho0'][i], dev) for i in idx])
-        Eg = [torch.stack([engine.as_device(E[i][0], dev) for i in idx])]
-        prepared.append((gen, rho, Eg, torch.cuda.Stream(device=dev)))
+    # the public uneven-batch call's groups (split: chains of N <= 32 packed
+    # block-diagonally, 64 // N to an instance), prepared once per precision
+    prepared = {}
+    for prec in ('split', 'fp64'):
+        prepared[prec] = [(g, torch.cuda.Stream(device=dev)) for g in
+                          engine.ragged_groups(w['H'], w['rho0'], w['c_ops'], E, prec, dev)]
 
     def run(steps, precision):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         a.record(main)
         fins = []
-        for gen, rho, Eg, st in prepared:
+        for g, st in prepared[precision]:
             st.wait_stream(main)
             with torch.cuda.stream(st):
-                fins.append(engine._launch(gen, rho, w['dt'], steps, Eg, precision=precision, defer=True))
-        for *_, st in prepared:
+                fins.append(engine._launch(g.gen, g.rho, w['dt'], steps, g.e_ops, precision=precision,
+                                           defer=True))
+        for _, st in prepared[precision]:
             main.wait_stream(st)
         b.record(main)
         torch.cuda.synchronize()
-        for (*_, st), fin in zip(prepared, fins):
+        for (_, st), fin in zip(prepared[precision], fins):
             with torch.cuda.stream(st):
                 fin(True)
         return a.elapsed_time(b) / 1e3
@@ -527,7 +524,9 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
     tf = run(steps_fp64, 'fp64')
     per_step = (t2 - t1) / (steps_split - steps_split // 2)
     small = [s for s in sorted(set(int(n) for n in ns)) if s <= 128] or [int(min(ns))]
-    sub = [int(i) for s in small for i in np.flatnonzero(ns == s)[:2]]
+    # a full block-diagonal pack plus one more chain for the packed sizes
+    sub = [int(i) for s in small
+           for i in np.flatnonzero(ns == s)[:(engine.PACK_DIM // s + 1 if 2 * s <= engine.PACK_DIM else 2)]]
     args = ([w['H'][i] for i in sub], [w['rho0'][i] for i in sub], w['dt'], err_steps,
             [w['c_ops'][i] for i in sub], [E[i] for i in sub])
     o64, _, _ = engine.propagate_ragged(*args, precision='fp64')
@@ -545,12 +544,13 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
                       'gpu_s_%d_steps' % steps_split: t2,
                       'algorithmic_tflops': flop / per_step / 1e12,
                       'path': 'streaming tcgen05 GEMMs (Heff rho, L rho L^dag), one launch '
-                              'sequence per size, sizes on concurrent streams'},
+                              'sequence per size (chains of N <= 32 packed block-diagonally, '
+                              '64 // N to an instance), sizes on concurrent streams'},
             'fp64_gpu': {'value': fp64_rate, 'steps': steps_fp64, 'gpu_s': tf},
             'speedup_vs_fp64_gpu': split_rate / fp64_rate,
             'split_max_population_error': err,
-            'error_sample': '%d chains (two of each N <= 128, else of the smallest N), %d steps'
-                            % (len(sub), err_steps)}
+            'error_sample': '%d chains (64 // N + 1 of each N <= 32, two of each N <= 128, else of '
+                            'the smallest N), %d steps' % (len(sub), err_steps)}
 
 
 def e2e_leg(wl, K, path, dev):

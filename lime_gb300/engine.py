@@ -492,6 +492,97 @@ def is_ragged(H) -> bool:
         not isinstance(x, (list, tuple)) and _dims(x) == 2 for x in H)
 
 
+# The tensor-core paths pad a chain to dimension 64 (the batched kernel's
+# fixed size, the streaming GEMMs' 64-wide K chunks).  An uneven batch packs
+# up to 64 // n chains of dimension n <= 32 block-diagonally into one
+# instance: the generator of a block-diagonal system (Heff, the collapse
+# operators, M) is block-diagonal, a block-diagonal state stays so, and the
+# zero blocks contribute exact zeros, so every chain evolves as it would
+# alone (up to the summation order inside the tensor-core accumulation).
+PACK_DIM = 64
+
+
+def pack_count(n: int, precision: str) -> int:
+    """Chains of dimension n per packed instance (1: not packed)."""
+    return PACK_DIM // n if precision == 'split' and 2 * n <= PACK_DIM else 1
+
+
+def _embed(blocks: torch.Tensor) -> torch.Tensor:
+    """(G, p, n, n) -> (G, p n, p n) block-diagonal."""
+    G, p, n, _ = blocks.shape
+    out = torch.zeros(G, p, n, p, n, dtype=blocks.dtype, device=blocks.device)
+    for s in range(p):
+        out[:, s, :, s, :] = blocks[:, s]
+    return out.reshape(G, p * n, p * n)
+
+
+class RaggedGroup:
+    """One batched launch of an uneven batch: instances ``idx`` (input
+    order) of dimension ``n``, ``pack`` of them block-diagonally to a
+    launched instance; ``gen``, ``rho``, ``e_ops`` are the launch's inputs."""
+
+    def __init__(self, idx, n, n_obs, pack, gen, rho, e_ops):
+        self.idx, self.n, self.n_obs, self.pack = idx, n, n_obs, pack
+        self.gen, self.rho, self.e_ops = gen, rho, e_ops
+
+    def unpack(self, o, s, r):
+        """Per-instance (obs, states, rho) from the launch's outputs."""
+        n, p, m = self.n, self.pack, self.n_obs
+        out = []
+        for j in range(len(self.idx)):
+            if p == 1:
+                out.append((o[j], None if s is None else s[j], r[j]))
+            else:
+                g, q = divmod(j, p)
+                out.append((o[g][..., q * m:(q + 1) * m], None,
+                            r[g][q * n:(q + 1) * n, q * n:(q + 1) * n]))
+        return out
+
+
+def ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision: str, device) -> list:
+    """Group an uneven batch by (dimension, operator count) and build each
+    group's generator, states and observables on ``device`` (packed
+    block-diagonally for precision='split' and n <= 32)."""
+    groups = {}
+    for i in range(len(H_list)):
+        h = H_list[i]
+        n = int(h.shape[-1]) if hasattr(h, 'shape') else int(np.shape(h)[-1])
+        groups.setdefault((n, len(c_ops_list[i])), []).append(i)
+    out = []
+    for (n, K), idx in sorted(groups.items()):
+        m = len(e_ops_list[idx[0]])
+        p = pack_count(n, precision)
+
+        def stacked(get):
+            x = torch.stack([as_device(get(i), device) for i in idx])
+            if p == 1:
+                return x
+            G = -(-len(idx) // p)
+            pad = torch.zeros((G * p - len(idx), n, n), dtype=x.dtype, device=device)
+            return _embed(torch.cat([x, pad]).reshape(G, p, n, n))
+
+        H = stacked(lambda i: H_list[i])
+        ops = [stacked(lambda i, k=k: c_ops_list[i][k]) for k in range(K)]
+        rho = stacked(lambda i: rho0_list[i])
+        if p == 1:
+            E = [torch.stack([as_device(e_ops_list[i][o], device) for i in idx]) for o in range(m)]
+        else:
+            # observable o of slot q: chain (g, q)'s operator in block q only
+            G = H.shape[0]
+            E = []
+            zero = torch.zeros((n, n), dtype=CDT, device=device)
+            for q in range(p):
+                for o in range(m):
+                    blocks = torch.zeros((G, p, n, n), dtype=CDT, device=device)
+                    for g in range(G):
+                        j = g * p + q
+                        blocks[g, q] = as_device(e_ops_list[idx[j]][o], device) if j < len(idx) else zero
+                    E.append(_embed(blocks))
+        gen = LindbladGenerator.build(H, ops, device=device)
+        out.append(RaggedGroup(idx, n, m, p, gen, rho, E))
+    return out
+
+
 def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None,
                      e_ops_list=None, states_every: int = 0, precision: str = 'fp64',
                      trace_tol: float | None = None, obs_every: int = 1, device=None):
@@ -500,12 +591,14 @@ def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None
     n_i x n_i operators; every instance has the same number of observables).
 
     Instances with equal dimension and operator counts are stacked into one
-    batched launch; the launches of different dimensions run concurrently on
-    separate CUDA streams and the status words are checked once all are
-    enqueued.  ``precision``: 'fp64' or 'split' (the batched tensor-core
-    kernel where it applies, the streaming tensor-core GEMMs elsewhere).
-    Returns three lists in input order: observables
-    (n_steps // obs_every, n_obs), states or None, final rho.
+    batched launch (with precision='split', chains of dimension <= 32 are
+    packed block-diagonally, 64 // n to an instance); the launches of
+    different dimensions run concurrently on separate CUDA streams and the
+    status words are checked once all are enqueued.  ``precision``: 'fp64'
+    or 'split' (the batched tensor-core kernel where it applies, the
+    streaming tensor-core GEMMs elsewhere).  Returns three lists in input
+    order: observables (n_steps // obs_every, n_obs), states or None, final
+    rho.
     """
     B = len(H_list)
     if len(rho0_list) != B:
@@ -518,34 +611,20 @@ def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None
     if len(n_obs) > 1:
         raise ValueError('every instance needs the same number of observables')
     device = _dev(device)
-    groups = {}
-    for i in range(B):
-        h = H_list[i]
-        n = int(h.shape[-1]) if hasattr(h, 'shape') else int(np.shape(h)[-1])
-        key = (n, len(c_ops_list[i]))
-        groups.setdefault(key, []).append(i)
     main = torch.cuda.current_stream(device)
     pending = []
-    for (n, K), idx in sorted(groups.items()):
+    for grp in ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision, device):
         st = torch.cuda.Stream(device=device)
         st.wait_stream(main)
         with torch.cuda.stream(st):
-            H = torch.stack([as_device(H_list[i], device) for i in idx])
-            ops = [torch.stack([as_device(c_ops_list[i][k], device) for i in idx]) for k in range(K)]
-            gen = LindbladGenerator.build(H, ops, device=device)
-            rho = torch.stack([as_device(rho0_list[i], device) for i in idx])
-            E = [torch.stack([as_device(e_ops_list[i][o], device) for i in idx])
-                 for o in range(len(e_ops_list[idx[0]]))]
-            fin = _launch(gen, rho, dt, n_steps, E, states_every=states_every, precision=precision,
-                          trace_tol=trace_tol, obs_every=obs_every, defer=True)
-        pending.append((idx, st, fin))
+            fin = _launch(grp.gen, grp.rho, dt, n_steps, grp.e_ops, states_every=states_every,
+                          precision=precision, trace_tol=trace_tol, obs_every=obs_every, defer=True)
+        pending.append((grp, st, fin))
     obs, states, rhos = [None] * B, [None] * B, [None] * B
-    for idx, st, fin in pending:
+    for grp, st, fin in pending:
         main.wait_stream(st)
         with torch.cuda.stream(st):
-            o, s, r = fin(True)
-        for j, i in enumerate(idx):
-            obs[i] = o[j]
-            states[i] = None if s is None else s[j]
-            rhos[i] = r[j]
+            res = grp.unpack(*fin(True))
+        for i, (o, s, r) in zip(grp.idx, res):
+            obs[i], states[i], rhos[i] = o, s, r
     return obs, states, rhos

@@ -91,3 +91,37 @@ def test_uneven_batch_argument_errors():
         engine.propagate_ragged(H, R[:1], 0.05, 3, C, E)
     with pytest.raises(ValueError):
         engine.propagate_ragged(H, R, 0.05, 3, C, [E[0], E[1][:1]])
+
+
+def test_packed_small_chains_split_vs_fp64():
+    """Chains of n <= 32 run block-diagonally packed on the tensor-core
+    paths (64 // n to an instance, the last pack partly empty): dense
+    collapse operators, an odd dimension, a non-Hermitian start and
+    dephasing-only chains (the batched kernel) all agree with FP64 per
+    instance."""
+    from lime_gb300 import engine
+    rng = np.random.default_rng(17)
+    sizes = [5] * 13 + [8] * 9 + [32] * 3
+    H, C, R, E = _uneven(sizes, 23)
+    psi = rng.normal(size=5) + 1j * rng.normal(size=5)
+    phi = rng.normal(size=5) + 1j * rng.normal(size=5)
+    R[1] = np.outer(psi, phi.conj()) / (np.linalg.norm(psi) * np.linalg.norm(phi))   # non-Hermitian
+    o64, _, r64 = engine.propagate_ragged(H, R, 0.05, 120, C, E)
+    osp, _, rsp = engine.propagate_ragged(H, R, 0.05, 120, C, E, precision='split')
+    for i, n in enumerate(sizes):
+        assert osp[i].shape == o64[i].shape == (120, 2)
+        assert rsp[i].shape == (n, n)
+        assert np.max(np.abs((osp[i] - o64[i]).cpu().numpy())) < 1e-6
+        assert np.max(np.abs((rsp[i] - r64[i]).cpu().numpy())) < 1e-6
+
+    Hd, Cd, Rd, Ed = [], [], [], []
+    for n in [6] * 11 + [16] * 5:
+        Hd.append(chains.exciton_chain(n, rng.normal(0, 0.05, n), -0.1))
+        Cd.append(chains.dephasing_ops(n, 0.01))
+        Rd.append(chains.ground_dm(n, 1))
+        Ed.append(chains.population_ops(n)[:2])
+    o64, _, r64 = engine.propagate_ragged(Hd, Rd, 0.05, 150, Cd, Ed)
+    osp, _, rsp = engine.propagate_ragged(Hd, Rd, 0.05, 150, Cd, Ed, precision='split')
+    for i in range(len(Hd)):
+        assert np.max(np.abs((osp[i] - o64[i]).cpu().numpy())) < 1e-6
+        assert np.max(np.abs((rsp[i] - r64[i]).cpu().numpy())) < 1e-6
