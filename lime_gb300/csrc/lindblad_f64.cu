@@ -437,7 +437,9 @@ __global__ void __launch_bounds__(kThreads) lindblad_adjoint_f64_kernel(AdjArgs 
   }
 }
 
-// Heff = H - (i/2) sum_k L_k^dag L_k ;  M = sum_k l_k l_k^dag
+// Heff = H - (i/2) sum_k L_k^dag L_k ;  M = sum_k l_k l_k^dag.  When every
+// diagonal operator has at most one nonzero entry (site dephasing), the
+// off-diagonal terms l_k[i] conj(l_k[j]) are exact zeros and are not summed.
 __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
   const int b = blockIdx.x;
   const int n = d.n;
@@ -447,6 +449,16 @@ __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
   const double2* lg = d.l_diag ? reinterpret_cast<const double2*>(d.l_diag) + b * d.l_diag_stride : nullptr;
   double2* heff = reinterpret_cast<double2*>(d.heff) + b * nn;
   double2* M = reinterpret_cast<double2*>(d.m) + b * nn;
+  __shared__ int spread;   // some l_k has two or more nonzero entries
+  if (threadIdx.x == 0) spread = 0;
+  __syncthreads();
+  for (int k = threadIdx.x; k < d.k_diag; k += kThreads) {
+    const double2* l = lg + (int64_t)k * n;
+    int nz = 0;
+    for (int q = 0; q < n; ++q) nz += (l[q].x != 0.0 || l[q].y != 0.0) ? 1 : 0;
+    if (nz > 1) atomicOr(&spread, 1);
+  }
+  __syncthreads();
   for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
     const int i = (int)(e / n), j = (int)(e % n);
     double2 g = cz();  // (sum_k L_k^dag L_k)_ij
@@ -455,7 +467,8 @@ __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
       for (int q = 0; q < n; ++q) cfma(g, cconj(L[(int64_t)q * n + i]), L[(int64_t)q * n + j]);
     }
     double2 mm = cz();
-    for (int k = 0; k < d.k_diag; ++k) {
+    const int k_m = (spread || i == j) ? d.k_diag : 0;
+    for (int k = 0; k < k_m; ++k) {
       const double2* l = lg + (int64_t)k * n;
       cfma(mm, l[i], cconj(l[j]));
       if (i == j) g = cadd(g, make_double2(l[i].x * l[i].x + l[i].y * l[i].y, 0.0));
