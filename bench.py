@@ -55,6 +55,9 @@ def parse():
     p.add_argument('--no-adjoint', action='store_true')
     p.add_argument('--no-redfield', action='store_true')
     p.add_argument('--no-ragged', action='store_true')
+    p.add_argument('--no-rows', action='store_true', help='skip the small other-workload leg')
+    p.add_argument('--rows-only', action='store_true',
+                   help='run only the single-chain / driven / two-time leg and print its JSON')
     p.add_argument('--redfield-only', action='store_true',
                    help='run only the dense Redfield leg and print its JSON')
     p.add_argument('--ragged-only', action='store_true',
@@ -191,6 +194,10 @@ def gpu_arm(args, rank, world, local):
             print(json.dumps(ragged_leg(torch, dev, batch=args.ragged_batch,
                                         sizes=tuple(int(x) for x in args.ragged_sizes.split(',')))))
         return
+    if args.rows_only:
+        if rank == 0:
+            print(json.dumps(rows_leg(torch, dev)))
+        return
     if args.redfield_only:
         if rank == 0:
             print(json.dumps(redfield_leg(torch, dev, measured_peaks(), n=args.redfield_n,
@@ -269,6 +276,9 @@ def gpu_arm(args, rank, world, local):
     if not args.no_ragged and single:
         rag = ragged_leg(torch, dev, batch=args.ragged_batch,
                          sizes=tuple(int(x) for x in args.ragged_sizes.split(',')))
+    rows = None
+    if not args.no_rows and single:
+        rows = rows_leg(torch, dev)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -324,6 +334,7 @@ def gpu_arm(args, rank, world, local):
         'adjoint': adj,
         'redfield': red,
         'uneven_batch': rag,
+        'other_workloads': rows,
         'cpu_baseline': cpu,
     }
     if rank == 0:
@@ -551,6 +562,80 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
             'split_max_population_error': err,
             'error_sample': '%d chains (64 // N + 1 of each N <= 32, two of each N <= 128, else of '
                             'the smallest N), %d steps' % (len(sub), err_steps)}
+
+
+def rows_leg(torch, dev):
+    """The other workloads of the path at small sizes, FP64 and split
+    precision side by side (GPU time with CUDA events around each public
+    call, set-up included; split error against the FP64 path):
+    the single 16-site chain (2000 steps, 16 populations every step), the
+    driven Lindblad equation (64-site chain, H(t) = H0 - f(t) mu with a
+    periodic f, 256 initial states, 1000 steps) and the two-time
+    correlation <A(t) B(t+tau) C(t)> (16-site chain, 200 x 200)."""
+    import numpy as np
+    from lime_gb300 import chains, engine
+    from lime_gb300.oqs import Lindblad_solver
+
+    def timed(fn):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b) / 1e3
+
+    out = {}
+    # single chain (latency of one small instance)
+    w = chains.single_chain(n=16, n_steps=2000)
+    gen = engine.LindbladGenerator.build(w['H'], w['c_ops'], device=dev)
+    res = {}
+    for prec in ('fp64', 'split', 'fp64', 'split'):   # second pass timed
+        (o, _, _), t = timed(lambda: engine.propagate(gen, w['rho0'], w['dt'], w['Nt'], w['e_ops'],
+                                                      precision=prec))
+        res[prec] = (o, t)
+    out['single_chain_n16'] = {
+        'steps': w['Nt'], 'fp64_steps_per_s': w['Nt'] / res['fp64'][1],
+        'split_steps_per_s': w['Nt'] / res['split'][1],
+        'split_max_population_error': float((res['split'][0] - res['fp64'][0]).abs().max())}
+
+    # driven Lindblad: H(t) = H0 - f(t) mu, shared generator, a batch of starts
+    n, B, steps, dt = 64, 256, 1000, 0.05
+    rng = np.random.default_rng(20261204)
+    H0 = chains.exciton_chain(n, rng.normal(0, 0.05, n), -0.1)
+    mu = np.zeros((n, n), dtype=np.complex128)
+    mu[0, 1:] = mu[1:, 0] = rng.normal(1.0, 0.1, n - 1)
+    coef = 0.01 * np.cos(0.1 * dt * np.arange(1, steps + 1))[:, None]
+    gen = engine.LindbladGenerator.build(H0, chains.dephasing_ops(n, 0.01), device=dev)
+    drive = (torch.as_tensor(mu[None], device=dev), torch.as_tensor(coef, device=dev))
+    rho0 = torch.as_tensor(np.stack([chains.ground_dm(n, k % n) for k in range(B)]), device=dev)
+    pops = chains.population_ops(n)[:8]
+    res = {}
+    for prec in ('fp64', 'split'):
+        engine.propagate(gen, rho0, dt, 2, pops, drive=(drive[0], drive[1][:2]), precision=prec)
+        (o, _, _), t = timed(lambda: engine.propagate(gen, rho0, dt, steps, pops, drive=drive,
+                                                      precision=prec))
+        res[prec] = (o, t)
+    out['driven_n64_b256'] = {
+        'steps': steps, 'unit': 'instance-steps/s',
+        'fp64': B * steps / res['fp64'][1], 'split': B * steps / res['split'][1],
+        'speedup_vs_fp64_gpu': res['fp64'][1] / res['split'][1],
+        'split_max_population_error': float((res['split'][0] - res['fp64'][0]).abs().max())}
+
+    # two-time correlation (the Nt inner propagations as one batch)
+    w = chains.single_chain(n=16, n_steps=200)
+    a = np.zeros((16, 16), dtype=np.complex128)
+    a[0, 1:] = a[1:, 0] = 1.0
+    res = {}
+    for prec in ('fp64', 'split', 'fp64', 'split'):
+        sol = Lindblad_solver(w['H'], c_ops=w['c_ops'], precision=prec)
+        c, t = timed(lambda: sol.correlation_3op_2t(w['rho0'], [a, a, a], w['dt'], 200, 200))
+        res[prec] = (c, t)
+    c64, csp = res['fp64'][0], res['split'][0]
+    out['two_time_3op_n16'] = {
+        'nt': 200, 'ntau': 200, 'fp64_s': res['fp64'][1], 'split_s': res['split'][1],
+        'split_rel_error': float(np.max(np.abs(csp - c64)) / np.max(np.abs(c64)))}
+    return out
 
 
 def e2e_leg(wl, K, path, dev):

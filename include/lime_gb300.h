@@ -396,7 +396,17 @@ int lime_lindblad_rk4_f64_noalloc(const LimeLindbladDesc* d, void* stream);
  *                 2 dense: obs_ops [P|1][n_obs][n][n], Tr(E rho)
  *   obs_out       [B][n_steps / obs_every][n_obs] complex128
  *   ctas_per_sm   0 = default (2)
- * No workspace: state lives on chip for the whole launch.
+ *   n_drive       0, or the number of drive operators: the generator of step
+ *                 k is Heff - sum_d drive_coef[k][d] drive_ops[d] (the
+ *                 driven equation of lime/oqs.py:1691-1800, coefficients at
+ *                 the end of the step, held through its four stages)
+ *   drive_ops     [n_drive][n][n] complex128, shared by all instances
+ *   drive_coef    [n_steps][n_drive] real
+ *   workspace     n_drive > 0: lime_lindblad_split_workspace(n, param_batch,
+ *                 n_drive, n_steps) bytes, 256-byte aligned (fp32 pair
+ *                 copies of Heff, the drive operators and coefficients);
+ *                 scale_a_log2 must cover max_k |Heff - sum_d c_d(k) mu_d|
+ * Without a drive no workspace: state lives on chip for the whole launch.
  */
 typedef struct {
   int32_t n, batch, param_batch, n_steps;
@@ -409,8 +419,13 @@ typedef struct {
   const double* obs_ops;  int64_t obs_stride;
   double* obs_out;
   int32_t* status;
+  int32_t n_drive;
+  const double* drive_ops;
+  const double* drive_coef;
+  void* workspace;        size_t workspace_bytes;
 } LimeLindbladSplitDesc;
 
+size_t lime_lindblad_split_workspace(int32_t n, int32_t param_batch, int32_t n_drive, int32_t n_steps);
 int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream);
 
 /* ------------------------------------------------------------------ */

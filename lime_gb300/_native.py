@@ -84,7 +84,11 @@ class SplitDesc(ctypes.Structure):
                 ('m_diag', c_void_p), ('m_stride', c_int64),
                 ('obs_ops', c_void_p), ('obs_stride', c_int64),
                 ('obs_out', c_void_p),
-                ('status', c_void_p)]
+                ('status', c_void_p),
+                ('n_drive', c_int32),
+                ('drive_ops', c_void_p),
+                ('drive_coef', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
 
 
 class AdjointDesc(ctypes.Structure):
@@ -184,6 +188,7 @@ SIGNATURES = [
     ('lime_lindblad_adjoint_stream', c_int32, [ctypes.POINTER(AdjointStreamDesc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
+    ('lime_lindblad_split_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),
     ('lime_wait_selftest_workspace', c_size_t, []),
     ('lime_wait_selftest', c_int32, [c_int32, ctypes.c_uint32, c_void_p, c_void_p, c_void_p]),

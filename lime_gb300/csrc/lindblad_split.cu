@@ -40,6 +40,14 @@
 // (B^T row i = [Re rho[i][:], -Im rho[i][:]]).  Observables, the trace check
 // and the final state are produced in FP64 from hi + lo.
 //
+// Drive (template kDrive).  Heff(t) = Heff - sum_d c_d(t) mu_d, with c_d
+// held through the four stages of a step (lime/oqs.py:1691-1800): the A
+// operand is split again at the start of every step, from fp32 hi/lo pairs
+// of Heff, mu_d and c_d (prepared once per call in the workspace) in
+// double-float arithmetic (~46 bits, FP64 being slow on this part), with
+// each row's fixed-point quantum taken once from a bound of the row over
+// the whole drive (max |Heff row| + sum_d max_t |c_d| max |mu_d row|).
+//
 // Units.  Each thread keeps its state component already in B units
 // (R = +-2^b rho, the sign of the B^T row it writes) and its RK4 sums in
 // accumulator units (X = 2^(a+b) Heff rho): the conversion factors are powers
@@ -88,6 +96,15 @@ struct Args {
   double2* obs_out;
   int32_t* status;
   uint32_t max_wait;
+  // drive (kDrive): operators, fp32 pairs [P|1][2][64][64] of Heff and
+  // [n_drive][2][64][64] of mu_d (component 0 = re, 1 = im, zero padded),
+  // coefficient pairs [n_steps][n_drive] and max_t |c_d|
+  int n_drive;
+  const double2* drive_ops;
+  const float2* heff_pair; int heff_pair_count;
+  const float2* drive_pair;
+  const float2* coef_pair;
+  const double* coef_max;
 };
 
 __device__ __forceinline__ double block_sum(double v, double* red, int t) {
@@ -153,6 +170,32 @@ __device__ __forceinline__ void store_b8(Smem& S, uint32_t off, const float* x, 
   *reinterpret_cast<uint4*>(S.bop[1] + off) = make_uint4(h1[0], h1[1], h1[2], h1[3]);
 }
 
+// x -= c * m on double-float pairs (x = xh + xl, c = ch + cl, m = mh + ml;
+// the product to ~46 bits, the difference by an exact two-sum).
+__device__ __forceinline__ void df_sub_prod(float& xh, float& xl, float ch, float cl, float mh, float ml) {
+  const float ph = __fmul_rn(ch, mh);
+  const float pe = __fmaf_rn(ch, mh, -ph);
+  const float pl = __fmaf_rn(ch, ml, __fmaf_rn(cl, mh, pe));
+  const float sm = __fsub_rn(xh, ph);
+  const float bb = __fsub_rn(sm, xh);
+  const float er = __fadd_rn(__fsub_rn(xh, __fsub_rn(sm, bb)), __fsub_rn(-ph, bb));
+  xh = sm;
+  xl = __fadd_rn(__fsub_rn(xl, pl), er);
+}
+
+// x = xh + xl (scaled, |x| < 128 q) -> a0 = nearest multiple of q clamped to
+// |a0| <= qmax = 127 q (0 for a negligible row) + fp16 residuals a1, a2.
+// xh - a0 is exact (both multiples of ulp(xh), difference <= q).
+__device__ __forceinline__ void split_a32(float xh, float xl, float magic, float qmax, __half& a0, __half& a1,
+                                          __half& a2) {
+  float v0 = __fsub_rn(__fadd_rn(xh, magic), magic);
+  v0 = fminf(fmaxf(v0, -qmax), qmax);
+  const float r = __fadd_rn(__fsub_rn(xh, v0), xl);
+  a0 = __float2half_rn(v0);
+  a1 = __float2half_rn(r);
+  a2 = __float2half_rn(__fsub_rn(r, __half2float(a1)));
+}
+
 // Issue one MMA pass (thread 0) and commit it to mbar; every thread then
 // waits on mbar itself (bounded), and the next __syncthreads_or turns any
 // thread's timeout into a common abort.  No thread can fall two phases
@@ -183,6 +226,7 @@ __device__ __forceinline__ void mma_pass(uint32_t tbase, uint64_t desc_b0, uint6
   tc::mma_commit(mbar);
 }
 
+template <bool kDrive>
 __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a) {
   extern __shared__ uint8_t smem_raw[];
   Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -227,8 +271,28 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
     const double2* heff = a.heff + p * a.heff_stride;
     const float mi = (a.m_diag && i < n) ? (float)a.m_diag[p * a.m_stride + i] : 0.f;
 
+    // ---- driven: the row's quantum from its bound over the whole drive; the
+    // A pieces are written at the start of every step ----
+    float magic_a = 0.f, qmax_a = 0.f;
+    if (kDrive) {
+      double rmax = 0.0;
+      for (int k = 0; k < 128; ++k) rmax = fmax(rmax, fabs(a_elem(heff, n, i, k, is_re)));
+      for (int dd = 0; dd < a.n_drive; ++dd) {
+        double mr = 0.0;
+        for (int k = 0; k < 128; ++k) mr = fmax(mr, fabs(a_elem(a.drive_ops + (int64_t)dd * n * n, n, i, k, is_re)));
+        rmax += a.coef_max[dd] * mr;
+      }
+      rmax *= a.sa_d;
+      if (rmax >= 0x1p-18) {
+        const int e = ilogb(rmax);
+        magic_a = ldexpf(1.5f, e - 6 + 23);
+        qmax_a = ldexpf(127.f, e - 6);
+      } else {
+        magic_a = 12582912.f;   // 1.5 * 2^23: rounds to integers, then clamped to 0
+      }
+    }
     // ---- A operand: scaled Heff block row r -> TMEM as A0 + A1 + A2 (this thread: k in [64h, 64h+64)) ----
-    {
+    if (!kDrive) {
       double rmax = 0.0;
       for (int k = 0; k < 128; ++k) rmax = fmax(rmax, fabs(a_elem(heff, n, i, k, is_re) * a.sa_d));
       double q = 1.0, inv_q = 0.0;   // inv_q = 0: no fixed-point part for negligible rows
@@ -298,6 +362,44 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
 
 #pragma unroll 1
     for (int step = 0; step < a.n_steps; ++step) {
+      if (kDrive) {
+        // A(t) = 2^a (Heff - sum_d c_d(t) mu_d) for this step (the previous
+        // step's MMAs, the last readers of TMEM A, have completed: every
+        // thread waited on them)
+        const int comp = is_re ? (h ? 0 : 1) : (h ? 1 : 0);   // Xr rows [Hr, -Hi], Xi rows [Hi, Hr]
+        const float ssa = ((!is_re && h) ? -1.f : 1.f) * (float)a.sa_d;
+        const int pp = a.heff_pair_count > 1 ? p : 0;
+        const float2* hrow = a.heff_pair + ((size_t)(pp * 2 + comp) * 64 + i) * 64;
+        const float2* cst = a.coef_pair + (size_t)(a.step0 + step) * a.n_drive;
+#pragma unroll 1
+        for (int qq = 0; qq < 2; ++qq) {
+          uint32_t p0[16], p1[16], p2[16];
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const int kk = qq * 32 + 2 * c;
+            const float4 hv = *reinterpret_cast<const float4*>(hrow + kk);
+            float x0h = hv.x, x0l = hv.y, x1h = hv.z, x1l = hv.w;
+            for (int dd = 0; dd < a.n_drive; ++dd) {
+              const float2 cd = cst[dd];
+              const float4 mv =
+                  *reinterpret_cast<const float4*>(a.drive_pair + ((size_t)(dd * 2 + comp) * 64 + i) * 64 + kk);
+              df_sub_prod(x0h, x0l, cd.x, cd.y, mv.x, mv.y);
+              df_sub_prod(x1h, x1l, cd.x, cd.y, mv.z, mv.w);
+            }
+            __half u0, u1, u2, w0, w1, w2;
+            split_a32(x0h * ssa, x0l * ssa, magic_a, qmax_a, u0, u1, u2);
+            split_a32(x1h * ssa, x1l * ssa, magic_a, qmax_a, w0, w1, w2);
+            p0[c] = pack_half2(u0, w0);
+            p1[c] = pack_half2(u1, w1);
+            p2[c] = pack_half2(u2, w2);
+          }
+          const uint32_t col = 32 * h + 16 * qq;
+          tc::tmem_st16(lane_addr + kColA0 + col, p0);
+          tc::tmem_st16(lane_addr + kColA1 + col, p1);
+          tc::tmem_st16(lane_addr + kColA2 + col, p2);
+        }
+        tc::tmem_wait_st();
+      }
 #pragma unroll 1
       for (int s = 0; s < 4; ++s, ++g) {
         // ---- pass 1: small products into D ----
@@ -484,12 +586,69 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
   }
 }
 
+// ---------------------------------------------------------------- drive preparation
+// Workspace of a driven call: fp32 hi/lo pairs of Heff ([P|1][2][64][64]),
+// of the drive operators ([n_drive][2][64][64]) and of the coefficients
+// ([n_steps][n_drive]), and max_t |c_d| ([n_drive] doubles).
+struct DriveWs {
+  size_t ops, coef, cmax, total;
+};
+static DriveWs drive_ws(int P, int n_drive, int n_steps) {
+  auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
+  DriveWs w;
+  w.ops = al((size_t)P * 2 * 4096 * sizeof(float2));
+  w.coef = w.ops + al((size_t)n_drive * 2 * 4096 * sizeof(float2));
+  w.cmax = w.coef + al((size_t)n_steps * n_drive * sizeof(float2));
+  w.total = w.cmax + al((size_t)n_drive * sizeof(double));
+  return w;
+}
+
+// count matrices (n x n, stride elements apart) -> [count][2][64][64] pairs, zero padded
+__global__ void pair_kernel(const double2* src, int64_t stride, int count, int n, float2* dst) {
+  const int64_t total = (int64_t)count * 4096;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / 4096), ij = (int)(e % 4096), i = ij / 64, j = ij % 64;
+    double2 v = make_double2(0.0, 0.0);
+    if (i < n && j < n) v = src[c * stride + (int64_t)i * n + j];
+    const float rh = (float)v.x, ih = (float)v.y;
+    dst[((int64_t)c * 2 + 0) * 4096 + ij] = make_float2(rh, (float)(v.x - (double)rh));
+    dst[((int64_t)c * 2 + 1) * 4096 + ij] = make_float2(ih, (float)(v.y - (double)ih));
+  }
+}
+
+// one block per drive operator: coefficient pairs and max_t |c_d|
+__global__ void coef_kernel(const double* coef, int n_steps, int n_drive, float2* cp, double* cmax) {
+  __shared__ double red[32];
+  const int dd = blockIdx.x;
+  double m = 0.0;
+  for (int s = threadIdx.x; s < n_steps; s += blockDim.x) {
+    const double v = coef[(int64_t)s * n_drive + dd];
+    const float hv = (float)v;
+    cp[(int64_t)s * n_drive + dd] = make_float2(hv, (float)(v - (double)hv));
+    m = fmax(m, fabs(v));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, red[w]);
+    cmax[dd] = r;
+  }
+}
+
 }  // namespace split
 }  // namespace lime
 
 using namespace lime;
 
 static int g_num_sms = 0;
+
+extern "C" size_t lime_lindblad_split_workspace(int32_t n, int32_t param_batch, int32_t n_drive, int32_t n_steps) {
+  if (n <= 0 || param_batch <= 0 || n_drive < 0 || n_steps < 0) return 0;
+  if (n_drive == 0) return 0;
+  return split::drive_ws(param_batch, n_drive, n_steps).total;
+}
 
 extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream) {
   if (!d) return LIME_ERR_ARG;
@@ -506,6 +665,13 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   const int pb = d->param_batch > 0 ? d->param_batch : d->batch;
   if (pb > d->batch) return LIME_ERR_ARG;
   if (!(d->dt == d->dt)) return LIME_ERR_ARG;
+  if (d->n_drive < 0) return LIME_ERR_ARG;
+  if (d->n_drive > 0) {
+    if (!d->drive_ops || !d->drive_coef || !d->workspace) return LIME_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(d->workspace) & 255) != 0) return LIME_ERR_ARG;
+    if (d->workspace_bytes < lime_lindblad_split_workspace(d->n, pb, d->n_drive, d->n_steps))
+      return LIME_ERR_WORKSPACE;
+  }
   if (d->n_steps == 0) return LIME_OK;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -539,20 +705,43 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   a.obs_out = reinterpret_cast<double2*>(d->obs_out);
   a.status = d->status;
   a.max_wait = 1u << 26;
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool driven = d->n_drive > 0;
+  if (driven) {
+    const split::DriveWs w = split::drive_ws(pb, d->n_drive, d->n_steps);
+    uint8_t* ws = static_cast<uint8_t*>(d->workspace);
+    const int hp = d->heff_stride == 0 ? 1 : pb;
+    a.n_drive = d->n_drive;
+    a.drive_ops = reinterpret_cast<const double2*>(d->drive_ops);
+    a.heff_pair = reinterpret_cast<const float2*>(ws);
+    a.heff_pair_count = hp;
+    a.drive_pair = reinterpret_cast<const float2*>(ws + w.ops);
+    a.coef_pair = reinterpret_cast<const float2*>(ws + w.coef);
+    a.coef_max = reinterpret_cast<const double*>(ws + w.cmax);
+    split::pair_kernel<<<304, 256, 0, st>>>(a.heff, d->heff_stride, hp, d->n, reinterpret_cast<float2*>(ws));
+    LIME_CUDA_TRY(cudaGetLastError());
+    split::pair_kernel<<<64, 256, 0, st>>>(a.drive_ops, (int64_t)d->n * d->n, d->n_drive, d->n,
+                                           reinterpret_cast<float2*>(ws + w.ops));
+    LIME_CUDA_TRY(cudaGetLastError());
+    split::coef_kernel<<<d->n_drive, 256, 0, st>>>(d->drive_coef, d->n_steps, d->n_drive,
+                                                   reinterpret_cast<float2*>(ws + w.coef),
+                                                   reinterpret_cast<double*>(ws + w.cmax));
+    LIME_CUDA_TRY(cudaGetLastError());
+    count_launch(3);
+  }
   const int ctas_per_sm = d->ctas_per_sm > 0 ? d->ctas_per_sm : 2;
   const int grid = (int)((d->batch < ctas_per_sm * g_num_sms) ? d->batch : ctas_per_sm * g_num_sms);
   const size_t smem = sizeof(split::Smem) + 1024;
-  LIME_CUDA_TRY(cudaFuncSetAttribute(split::lindblad_rk4_split_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto kern = driven ? split::lindblad_rk4_split_kernel<true> : split::lindblad_rk4_split_kernel<false>;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // bounded launches: about 2^22 instance-steps per launch
   const double per_cta = (double)((d->batch + grid - 1) / grid);
   int chunk = (int)fmax(1.0, fmin((double)d->n_steps, 4194304.0 / (per_cta * grid)));
   if (a.obs_every > 1) chunk = ((chunk + a.obs_every - 1) / a.obs_every) * a.obs_every;
-  cudaStream_t st = (cudaStream_t)stream;
   for (int s0 = 0; s0 < d->n_steps; s0 += chunk) {
     a.step0 = s0;
     a.n_steps = (d->n_steps - s0 < chunk) ? d->n_steps - s0 : chunk;
-    split::lindblad_rk4_split_kernel<<<grid, split::kThreads, smem, st>>>(a);
+    kern<<<grid, split::kThreads, smem, st>>>(a);
     LIME_CUDA_TRY(cudaGetLastError());
     count_launch();
   }

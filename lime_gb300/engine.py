@@ -264,11 +264,14 @@ def _split_obs(e_ops, n, P, device):
 
 def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
                obs_every: int, trace_tol: float, param_batch: int, events=None,
-               ctas_per_sm: int = 0):
+               ctas_per_sm: int = 0, drive=None):
     """The batched tensor-core kernel (n <= 64, diagonal collapse operators).
     State scale: sqrt(n) ||rho(0)||_F (a bound of |rho_ij(t)|: the trace
     norm contracts) at 2^13; the kernel picks each B row's fixed-point
-    quantum from the previous stage's row bound."""
+    quantum from the previous stage's row bound.  ``drive`` = (ops
+    (n_drive, n, n), coef (n_steps, n_drive)): Heff(t) = Heff - sum_d
+    coef[k, d] ops[d], re-split on the device every step; the A scale then
+    covers max|Heff| + sum_d max|coef_d| max|ops_d|."""
     lib = nat.require_device()
     why = split_supported(gen)
     if why is not None:
@@ -281,6 +284,14 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
     if gen.m is not None:
         m_diag = torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous()
     amax = float(gen.heff.abs().max().item())
+    ws = None
+    if drive is not None:
+        dops, dcoef = drive
+        if dcoef.shape[0] < n_steps:
+            raise ValueError('drive coefficients cover %d steps, %d requested' % (dcoef.shape[0], n_steps))
+        amax += float((dcoef.abs().amax(0) * dops.abs().amax((-2, -1))).sum().item())
+        ws = torch.empty(int(lib.lime_lindblad_split_workspace(n, param_batch, dops.shape[0], n_steps)),
+                         dtype=torch.uint8, device=rho.device)
     rbound = float(torch.linalg.matrix_norm(rho).max().item()) * (n ** 0.5)
     sb = _pow2_exponent(8192.0, rbound)
     d = nat.SplitDesc()
@@ -298,6 +309,9 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
         d.obs_ops, d.obs_stride = Et.data_ptr(), obs_stride
     d.obs_out = obs_out.data_ptr()
     d.status = status.data_ptr()
+    if drive is not None:
+        d.n_drive, d.drive_ops, d.drive_coef = dops.shape[0], dops.data_ptr(), dcoef.data_ptr()
+        d.workspace, d.workspace_bytes = ws.data_ptr(), ws.numel()
     if events is not None:
         events[0].record()
     nat.check(lib.lime_lindblad_rk4_split(d, _stream_ptr()), 'lime_lindblad_rk4_split')
@@ -430,10 +444,10 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
         if states_every:
             raise ValueError('precision="split" keeps the state on chip; states_every is not '
                              'supported (use precision="fp64" for rholist output)')
-        if split_supported(gen) is None and drive is None:
+        if split_supported(gen) is None:
             tol = 1e-5 if trace_tol is None else trace_tol
             o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
-                                      param_batch=B, events=events)
+                                      param_batch=B, events=events, drive=drive)
         else:
             o, s, status, work, redo = _run_stream(gen, work, dt, n_steps, e_ops, obs_every,
                                                    param_batch=B, events=events, drive=drive,
