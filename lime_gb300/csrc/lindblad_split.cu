@@ -105,6 +105,9 @@ struct Args {
   const float2* drive_pair;
   const float2* coef_pair;
   const double* coef_max;
+  // per (matrix, component, row): first and last nonzero column (x > y: none)
+  const int2* heff_rng;
+  const int2* drive_rng;
 };
 
 __device__ __forceinline__ double block_sum(double v, double* red, int t) {
@@ -370,6 +373,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         const float ssa = ((!is_re && h) ? -1.f : 1.f) * (float)a.sa_d;
         const int pp = a.heff_pair_count > 1 ? p : 0;
         const float2* hrow = a.heff_pair + ((size_t)(pp * 2 + comp) * 64 + i) * 64;
+        const int2 hr = a.heff_rng[(pp * 2 + comp) * 64 + i];
         const float2* cst = a.coef_pair + (size_t)(a.step0 + step) * a.n_drive;
 #pragma unroll 1
         for (int qq = 0; qq < 2; ++qq) {
@@ -377,14 +381,21 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
 #pragma unroll
           for (int c = 0; c < 16; ++c) {
             const int kk = qq * 32 + 2 * c;
-            const float4 hv = *reinterpret_cast<const float4*>(hrow + kk);
-            float x0h = hv.x, x0l = hv.y, x1h = hv.z, x1l = hv.w;
+            // entries outside a row's nonzero range are zero: not loaded
+            float x0h = 0.f, x0l = 0.f, x1h = 0.f, x1l = 0.f;
+            if (kk + 1 >= hr.x && kk <= hr.y) {
+              const float4 hv = *reinterpret_cast<const float4*>(hrow + kk);
+              x0h = hv.x; x0l = hv.y; x1h = hv.z; x1l = hv.w;
+            }
             for (int dd = 0; dd < a.n_drive; ++dd) {
-              const float2 cd = cst[dd];
-              const float4 mv =
-                  *reinterpret_cast<const float4*>(a.drive_pair + ((size_t)(dd * 2 + comp) * 64 + i) * 64 + kk);
-              df_sub_prod(x0h, x0l, cd.x, cd.y, mv.x, mv.y);
-              df_sub_prod(x1h, x1l, cd.x, cd.y, mv.z, mv.w);
+              const int2 mr = a.drive_rng[(dd * 2 + comp) * 64 + i];
+              if (kk + 1 >= mr.x && kk <= mr.y) {
+                const float2 cd = cst[dd];
+                const float4 mv =
+                    *reinterpret_cast<const float4*>(a.drive_pair + ((size_t)(dd * 2 + comp) * 64 + i) * 64 + kk);
+                df_sub_prod(x0h, x0l, cd.x, cd.y, mv.x, mv.y);
+                df_sub_prod(x1h, x1l, cd.x, cd.y, mv.z, mv.w);
+              }
             }
             __half u0, u1, u2, w0, w1, w2;
             split_a32(x0h * ssa, x0l * ssa, magic_a, qmax_a, u0, u1, u2);
@@ -589,9 +600,11 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
 // ---------------------------------------------------------------- drive preparation
 // Workspace of a driven call: fp32 hi/lo pairs of Heff ([P|1][2][64][64]),
 // of the drive operators ([n_drive][2][64][64]) and of the coefficients
-// ([n_steps][n_drive]), and max_t |c_d| ([n_drive] doubles).
+// ([n_steps][n_drive]), max_t |c_d| ([n_drive] doubles), and the nonzero
+// column range of every row of the pair arrays ([P|1][2][64] and
+// [n_drive][2][64] int2).
 struct DriveWs {
-  size_t ops, coef, cmax, total;
+  size_t ops, coef, cmax, hrng, drng, total;
 };
 static DriveWs drive_ws(int P, int n_drive, int n_steps) {
   auto al = [](size_t x) { return (x + 255) & ~size_t(255); };
@@ -599,8 +612,27 @@ static DriveWs drive_ws(int P, int n_drive, int n_steps) {
   w.ops = al((size_t)P * 2 * 4096 * sizeof(float2));
   w.coef = w.ops + al((size_t)n_drive * 2 * 4096 * sizeof(float2));
   w.cmax = w.coef + al((size_t)n_steps * n_drive * sizeof(float2));
-  w.total = w.cmax + al((size_t)n_drive * sizeof(double));
+  w.hrng = w.cmax + al((size_t)n_drive * sizeof(double));
+  w.drng = w.hrng + al((size_t)P * 2 * 64 * sizeof(int2));
+  w.total = w.drng + al((size_t)n_drive * 2 * 64 * sizeof(int2));
   return w;
+}
+
+// one thread per row of a [count][2][64][64] pair array: its first and last
+// nonzero column ((64, -1) for an all-zero row)
+__global__ void range_kernel(const float2* pairs, int rows, int2* rng) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  const float2* row = pairs + (size_t)r * 64;
+  int lo = 64, hi = -1;
+  for (int j = 0; j < 64; ++j) {
+    const float2 v = row[j];
+    if (v.x != 0.f || v.y != 0.f) {
+      lo = min(lo, j);
+      hi = j;
+    }
+  }
+  rng[r] = make_int2(lo, hi);
 }
 
 // count matrices (n x n, stride elements apart) -> [count][2][64][64] pairs, zero padded
@@ -718,6 +750,8 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
     a.drive_pair = reinterpret_cast<const float2*>(ws + w.ops);
     a.coef_pair = reinterpret_cast<const float2*>(ws + w.coef);
     a.coef_max = reinterpret_cast<const double*>(ws + w.cmax);
+    a.heff_rng = reinterpret_cast<const int2*>(ws + w.hrng);
+    a.drive_rng = reinterpret_cast<const int2*>(ws + w.drng);
     split::pair_kernel<<<304, 256, 0, st>>>(a.heff, d->heff_stride, hp, d->n, reinterpret_cast<float2*>(ws));
     LIME_CUDA_TRY(cudaGetLastError());
     split::pair_kernel<<<64, 256, 0, st>>>(a.drive_ops, (int64_t)d->n * d->n, d->n_drive, d->n,
@@ -727,7 +761,13 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
                                                    reinterpret_cast<float2*>(ws + w.coef),
                                                    reinterpret_cast<double*>(ws + w.cmax));
     LIME_CUDA_TRY(cudaGetLastError());
-    count_launch(3);
+    split::range_kernel<<<(hp * 128 + 127) / 128, 128, 0, st>>>(a.heff_pair, hp * 128,
+                                                                reinterpret_cast<int2*>(ws + w.hrng));
+    LIME_CUDA_TRY(cudaGetLastError());
+    split::range_kernel<<<(d->n_drive * 128 + 127) / 128, 128, 0, st>>>(a.drive_pair, d->n_drive * 128,
+                                                                         reinterpret_cast<int2*>(ws + w.drng));
+    LIME_CUDA_TRY(cudaGetLastError());
+    count_launch(5);
   }
   const int ctas_per_sm = d->ctas_per_sm > 0 ? d->ctas_per_sm : 2;
   const int grid = (int)((d->batch < ctas_per_sm * g_num_sms) ? d->batch : ctas_per_sm * g_num_sms);
