@@ -301,6 +301,9 @@ typedef struct {
   int32_t n_drive;
   const double* drive_ops;
   const double* drive_coef;
+  /* a diagonal M (real M_ii, [P|1][n], stride n or 0) instead of m: the
+   * jump term then touches only the diagonal (pure dephasing) */
+  const double* m_diag;   int64_t m_diag_stride;
 } LimeLindbladStreamDesc;
 
 size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops);
@@ -344,6 +347,7 @@ typedef struct {
   double* grad_gamma;
   void* workspace;         size_t workspace_bytes;
   int32_t* status;
+  const double* m_diag;    int64_t m_diag_stride;   /* as in LimeLindbladStreamDesc (replaces m and m_adj) */
 } LimeLindbladAdjointStreamDesc;
 
 size_t lime_lindblad_adjoint_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t seg_steps);

@@ -149,7 +149,8 @@ class LindbladStreamDesc(ctypes.Structure):
                 ('obs_out', c_void_p),
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
                 ('status', c_void_p),
-                ('n_drive', c_int32), ('drive_ops', c_void_p), ('drive_coef', c_void_p)]
+                ('n_drive', c_int32), ('drive_ops', c_void_p), ('drive_coef', c_void_p),
+                ('m_diag', c_void_p), ('m_diag_stride', c_int64)]
 
 
 class AdjointStreamDesc(ctypes.Structure):
@@ -165,7 +166,8 @@ class AdjointStreamDesc(ctypes.Structure):
                 ('obs_grad', c_void_p),
                 ('grad_diag', c_void_p), ('grad_bond', c_void_p), ('grad_gamma', c_void_p),
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
-                ('status', c_void_p)]
+                ('status', c_void_p),
+                ('m_diag', c_void_p), ('m_diag_stride', c_int64)]
 
 
 # (name, restype, argtypes) of every exported symbol; tests check the header

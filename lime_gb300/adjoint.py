@@ -92,6 +92,10 @@ def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, 
     C = gsrc.shape[0]
     heff_adj = (-heff.mH).contiguous()
     m_adj = None if m is None else m.conj().contiguous()
+    # a diagonal M (pure dephasing) goes in as its real diagonal
+    m_diag = None
+    if m is not None and engine.is_diagonal(m):
+        m_diag = torch.diagonal(m, dim1=-2, dim2=-1).real.contiguous()
     shared = heff.shape[0] == 1
     G = 1 if shared else B
     # rho is scaled by its largest element over the checkpoints (the
@@ -116,7 +120,9 @@ def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, 
         d.ckpt = ckpts.data_ptr()
         d.heff, d.heff_stride = heff.data_ptr(), (0 if shared else N * N)
         d.heff_adj, d.heff_adj_stride = heff_adj.data_ptr(), (0 if shared else N * N)
-        if m is not None:
+        if m_diag is not None:
+            d.m_diag, d.m_diag_stride = m_diag.data_ptr(), (0 if m_diag.shape[0] == 1 else N)
+        elif m is not None:
             d.m, d.m_adj = m.data_ptr(), m_adj.data_ptr()
             d.m_stride = 0 if m.shape[0] == 1 else N * N
         if n_obs > 0:

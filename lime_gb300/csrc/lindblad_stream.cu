@@ -51,6 +51,8 @@ struct Args {
   float* Acc;
   const double2* m;                   // [P|1][n][n] or null
   int64_t m_stride;
+  const double* mdg;                  // diagonal M (real, [P|1][n]) instead of m, or null
+  int64_t mdg_stride;
   bool keep_s;                        // maintain the fp32 stage-input copy (Sc / Sn)
   const int* sb_exp_dev;              // GEMM 1: B scale exponent read from the device (or null: inv_sb)
   float* stage_store;                 // finish_kernel: also store the stage input here ([B][W][np]) or null
@@ -81,7 +83,18 @@ __device__ __forceinline__ void assemble_f_tr(const Args& a, int b, int jj, int 
 #pragma unroll
     for (int i = 0; i < 8; ++i) f[i] = __fadd_rn(f[i], __fsub_rn(tr[i], u[i]));
   }
-  if (a.m != nullptr && x < a.n) {
+  if (a.mdg != nullptr) {
+    // diagonal M: only (M o rho)_xx = M_xx rho_xx, real (the stage input's
+    // diagonal is real), so only the real column x meets it, in row x
+    if (!im && x < a.n && x >= y && x < y + 8) {
+      const double* Md = a.mdg + (a.mdg_stride ? (int64_t)(b % a.P) * a.mdg_stride : 0);
+      const float sxx = a.Sc[(size_t)b * inst_floats(a) + (size_t)x * np + x];
+      const float mr = (float)Md[x];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (y + i == x) f[i] = __fmaf_rn(mr, sxx, f[i]);
+    }
+  } else if (a.m != nullptr && x < a.n) {
     const double2* M = a.m + (a.m_stride ? (int64_t)(b % a.P) * a.m_stride : 0);
     const float* S = a.Sc + (size_t)b * inst_floats(a);
     float sr[8], si[8];
@@ -676,6 +689,7 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   if (d->n_ops > 0 && !d->l_ops) return LIME_ERR_ARG;
   if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
   if (d->heff_stride < 0 || d->l_stride < 0 || d->m_stride < 0 || d->obs_stride < 0) return LIME_ERR_ARG;
+  if (d->m_diag_stride < 0) return LIME_ERR_ARG;
   if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60 || d->scale_y_log2 < -60 || d->scale_y_log2 > 60)
     return LIME_ERR_ARG;
   if (d->n > 4096 || d->n_ops > 64) return LIME_ERR_UNSUPPORTED;
@@ -719,7 +733,10 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
                  (float)(d->dt / 6.0 - (double)(float)(d->dt / 6.0))};
   a.m = reinterpret_cast<const double2*>(d->m);
   a.m_stride = d->m_stride;
-  a.keep_s = a.m != nullptr;
+  a.mdg = d->m_diag;
+  a.mdg_stride = d->m_diag_stride;
+  if (a.mdg != nullptr) a.m = nullptr;
+  a.keep_s = a.m != nullptr || a.mdg != nullptr;
   a.stage_store = nullptr;
   a.sb_exp_dev = nullptr;
   a.status = d->status;
@@ -812,6 +829,7 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
   if (d->n_obs > 0 && (!d->obs_ops || !d->obs_grad)) return LIME_ERR_ARG;
   if ((d->m == nullptr) != (d->m_adj == nullptr)) return LIME_ERR_ARG;
   if (d->heff_stride < 0 || d->heff_adj_stride < 0 || d->m_stride < 0 || d->obs_stride < 0) return LIME_ERR_ARG;
+  if (d->m_diag_stride < 0) return LIME_ERR_ARG;
   if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60 || d->scale_l_log2 < -60 || d->scale_l_log2 > 60)
     return LIME_ERR_ARG;
   if (d->n > 4096) return LIME_ERR_UNSUPPORTED;
@@ -868,6 +886,10 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
   af.m = reinterpret_cast<const double2*>(d->m);
   aa.m = reinterpret_cast<const double2*>(d->m_adj);
   af.m_stride = aa.m_stride = d->m_stride;
+  // a real diagonal M is its own conjugate: both directions use it
+  af.mdg = aa.mdg = d->m_diag;
+  af.mdg_stride = aa.mdg_stride = d->m_diag_stride;
+  if (d->m_diag != nullptr) af.m = aa.m = nullptr;
   af.keep_s = aa.keep_s = true;
   af.sb_exp_dev = nullptr;
   aa.sb_exp_dev = J.sl_exp;

@@ -356,6 +356,10 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     scales = [_pow2_exponent(8192.0 / 1.25, pmax), _pow2_exponent(8192.0 / 1.25, lrow * pmax) if K else 0]
     heff_shared = gen.heff.shape[0] == 1
     l_shared = gen.l_dense is None or gen.l_dense.shape[0] == 1
+    # a diagonal M (pure dephasing) goes in as its real diagonal
+    m_diag = None
+    if gen.m is not None and is_diagonal(gen.m):
+        m_diag = torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous()
     G = 1 if (heff_shared and l_shared) else param_batch
     wsb = lib.lime_lindblad_stream_workspace(n, B, G, K)
     ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
@@ -372,7 +376,9 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
         d.dt = float(dt)
         d.rho = work.data_ptr()
         d.heff, d.heff_stride = gen.heff.data_ptr(), (0 if heff_shared else n * n)
-        if gen.m is not None:
+        if m_diag is not None:
+            d.m_diag, d.m_diag_stride = m_diag.data_ptr(), (0 if m_diag.shape[0] == 1 else n)
+        elif gen.m is not None:
             d.m, d.m_stride = gen.m.data_ptr(), (0 if gen.m.shape[0] == 1 else n * n)
         if K:
             d.l_ops, d.l_stride = gen.l_dense.data_ptr(), (0 if l_shared else K * n * n)
