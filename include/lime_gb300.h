@@ -348,6 +348,12 @@ typedef struct {
   void* workspace;         size_t workspace_bytes;
   int32_t* status;
   const double* m_diag;    int64_t m_diag_stride;   /* as in LimeLindbladStreamDesc (replaces m and m_adj) */
+  /* optional: the observable sources' coefficients in fp32, float pairs
+   * [P|1][n_obs][2][n][n] (same instance stride rule as obs_ops): for
+   * component c of element (row, x), (Re E_xr + Re E_rx, Im E_xr + Im E_rx) / 2
+   * (c = 0) and (Im E_rx - Im E_xr, Re E_xr - Re E_rx) / 2 (c = 1), so the
+   * source is Re g Q.x + Im g Q.y; NULL: formed from obs_ops in FP64 */
+  const float* obs_coef;
 } LimeLindbladAdjointStreamDesc;
 
 size_t lime_lindblad_adjoint_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t seg_steps);

@@ -167,7 +167,8 @@ class AdjointStreamDesc(ctypes.Structure):
                 ('grad_diag', c_void_p), ('grad_bond', c_void_p), ('grad_gamma', c_void_p),
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
                 ('status', c_void_p),
-                ('m_diag', c_void_p), ('m_diag_stride', c_int64)]
+                ('m_diag', c_void_p), ('m_diag_stride', c_int64),
+                ('obs_coef', c_void_p)]
 
 
 # (name, restype, argtypes) of every exported symbol; tests check the header

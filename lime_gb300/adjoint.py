@@ -85,6 +85,16 @@ def _pow2_scale(bound: float) -> int:
     return max(-60, min(60, int(math.floor(math.log2(8192.0 / (1.25 * bound))))))
 
 
+def _source_coef(Et: torch.Tensor) -> torch.Tensor:
+    """fp32 coefficient pairs of the observable sources (the kernel forms
+    Re g Q.x + Im g Q.y): Et (P|1, n_obs, N, N) -> (P|1, n_obs, 2, N, N, 2),
+    index [.., x, row] with A = E[x, row], B = E[row, x]."""
+    A, Bt = Et, Et.transpose(-1, -2)
+    re = torch.stack([(A.real + Bt.real) / 2, (A.imag + Bt.imag) / 2], -1)
+    im = torch.stack([(Bt.imag - A.imag) / 2, (A.real - Bt.real) / 2], -1)
+    return torch.stack([re, im], 2).to(torch.float32).contiguous()
+
+
 def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, B, N, max_retries=2):
     """The discrete adjoint on the tensor cores (lime_lindblad_adjoint_stream)."""
     lib = nat.require_device()
@@ -103,6 +113,7 @@ def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, 
     # the device from max |lam|
     pmax = float(torch.view_as_real(ckpts).abs().max().item())
     sb = _pow2_scale(pmax)
+    qcoef = _source_coef(Et) if n_obs > 0 else None
     wsb = lib.lime_lindblad_adjoint_stream_workspace(N, C, G, K)
     ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
     aligned = (ws.data_ptr() + 1023) // 1024 * 1024
@@ -128,6 +139,7 @@ def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, 
         if n_obs > 0:
             d.obs_ops, d.obs_stride = Et.data_ptr(), (0 if Et.shape[0] == 1 else n_obs * N * N)
             d.obs_grad = gsrc.data_ptr()
+            d.obs_coef = qcoef.data_ptr()
         d.grad_diag, d.grad_bond, d.grad_gamma = gd.data_ptr(), gb.data_ptr(), gg.data_ptr()
         d.workspace, d.workspace_bytes = aligned, wsb
         d.status = status.data_ptr()

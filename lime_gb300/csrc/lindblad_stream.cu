@@ -444,8 +444,12 @@ __global__ void adj_scale_kernel(AdjState j) {
 
 // Source of the observables recorded after this step, lam += Herm(g E^dag)
 // (torch's convention dL = Re sum conj(g) d obs), and max |lam| of the step.
+// Observable sources into the adjoint state: (g conj(E_ji) + conj(g) E_ij) / 2
+// per element (torch's convention dL = Re sum conj(g) d obs), formed in FP64
+// from E, or, with Q (obs_coef), as Re g Q.x + Im g Q.y from its fp32
+// coefficient pairs ([P|1][n_obs][component][x][row], two FMAs an element).
 __global__ void adj_source_kernel(Args a, AdjState j, int batch, const double2* E, int64_t e_stride, int n_obs,
-                                  const double2* gsrc, int n_slots, int slot) {
+                                  const double2* gsrc, int n_slots, int slot, const float2* Q) {
   const size_t runs = (size_t)a.W * (a.np / 8);
   const size_t total = (size_t)batch * runs;
   float mx = 0.f;
@@ -458,7 +462,28 @@ __global__ void adj_source_kernel(Args a, AdjState j, int batch, const double2* 
     const size_t e = (size_t)b * inst_floats(a) + (size_t)jj * a.np + y;
     float hi[8];
     sg::ld8(j.Lhi + e, hi);
-    if (slot >= 0 && x < a.n) {
+    if (slot >= 0 && x < a.n && Q != nullptr) {
+      float lo[8];
+      sg::ld8(j.Llo + e, lo);
+      const float2* Qb = Q + (e_stride ? (int64_t)(b % a.P) * n_obs * 2 * a.n * a.n : 0);
+      const double2* g = gsrc + ((size_t)b * n_slots + slot) * n_obs;
+      float src[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int o = 0; o < n_obs; ++o) {
+        const float gx = (float)g[o].x, gy = (float)g[o].y;
+        const float2* Qo = Qb + (((size_t)o * 2 + (im ? 1 : 0)) * a.n + x) * a.n + y;
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          if (y + i < a.n) {
+            const float2 q = Qo[i];
+            src[i] = __fmaf_rn(gx, q.x, __fmaf_rn(gy, q.y, src[i]));
+          }
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (y + i < a.n) hi[i] = rk4_final_f32(hi[i], 0.f, src[i], 1.f, 0.f, lo[i]);
+      sg::st8(j.Lhi + e, hi);
+      sg::st8(j.Llo + e, lo);
+    } else if (slot >= 0 && x < a.n) {
       float lo[8];
       sg::ld8(j.Llo + e, lo);
       const double2* Eb = E + (e_stride ? (int64_t)(b % a.P) * e_stride : 0);
@@ -955,7 +980,8 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
       aa.Sn = Sbuf[c];
       lsm::adj_source_kernel<<<eb, 256, 0, st>>>(aa, J, B, reinterpret_cast<const double2*>(d->obs_ops),
                                                   d->obs_stride, d->n_obs,
-                                                  reinterpret_cast<const double2*>(d->obs_grad), n_slots, slot);
+                                                  reinterpret_cast<const double2*>(d->obs_grad), n_slots, slot,
+                                                  reinterpret_cast<const float2*>(d->obs_coef));
       LIME_CUDA_TRY(cudaGetLastError());
       lsm::adj_scale_kernel<<<1, 1, 0, st>>>(J);
       LIME_CUDA_TRY(cudaGetLastError());
