@@ -139,7 +139,8 @@ def _backward_split(heff, m, ckpts, gsrc, Et, n_obs, dt, n_steps, obs_every, K, 
         if n_obs > 0:
             d.obs_ops, d.obs_stride = Et.data_ptr(), (0 if Et.shape[0] == 1 else n_obs * N * N)
             d.obs_grad = gsrc.data_ptr()
-            d.obs_coef = qcoef.data_ptr()
+            if qcoef is not None:
+                d.obs_coef = qcoef.data_ptr()
         d.grad_diag, d.grad_bond, d.grad_gamma = gd.data_ptr(), gb.data_ptr(), gg.data_ptr()
         d.workspace, d.workspace_bytes = aligned, wsb
         d.status = status.data_ptr()

@@ -178,6 +178,21 @@ def test_split_adjoint_matches_fp64_adjoint(case):
         assert rel(got, ref) < GTOL, (case, rel(got, ref))
 
 
+def test_split_adjoint_source_paths_agree(monkeypatch):
+    """The adjoint's observable sources from the fp32 coefficient pairs (the
+    host's default) and formed in FP64 inside the kernel (no obs_coef) give
+    the same gradients."""
+    from lime_gb300 import adjoint
+    dev = torch.device('cuda')
+    c = _setup_absorption(dev)
+    o1, g1, w = _grads(c, 'split', 0.05, 29, 8)
+    monkeypatch.setattr(adjoint, '_source_coef', lambda Et: None)
+    o2, g2, _ = _grads(c, 'split', 0.05, 29, 8, w)
+    assert rel(o1, o2) < 1e-12
+    for a, b in zip(g1, g2):
+        assert rel(a, b) < 1e-6, rel(a, b)
+
+
 def test_split_adjoint_large_chain():
     """n = 70 (> 64): the forward runs on the streaming path too."""
     dev = torch.device('cuda')
