@@ -385,6 +385,9 @@ __global__ void observe_kernel(Args a, const double2* E, int64_t e_stride, int n
   for (int q = threadIdx.x; q < a.n * a.n; q += blockDim.x) {
     const int x = q / a.n, y = q - x * a.n;
     const double2 ev = Eo[(size_t)x * a.n + y];
+    // a zero entry adds exactly zero (projectors and dipoles are sparse);
+    // non-finite states are flagged by the stage kernels
+    if (ev.x == 0.0 && ev.y == 0.0) continue;
     const size_t er = base + (size_t)x * a.np + y, ei = base + (size_t)(a.np + x) * a.np + y;
     const double pr = (double)a.Phi[er] + (double)a.Plo[er];
     const double pi = (double)a.Phi[ei] + (double)a.Plo[ei];
