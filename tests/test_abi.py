@@ -95,6 +95,20 @@ def test_stream_and_redfield_workspace_queries(lib):
     assert r(8, 64, 200) > r(8, 64, 100) > r(8, 64, 0)
 
 
+def test_split_drive_workspace_query(lib):
+    # no drive: no workspace; otherwise fp32 pairs of Heff ([P][2][64][64]),
+    # of the drive operators, the coefficients, their maxima and row ranges
+    w = lib.lime_lindblad_split_workspace
+    assert w(64, 16, 0, 100) == 0 and w(0, 1, 1, 1) == 0 and w(8, 0, 1, 1) == 0
+    pair = 2 * 64 * 64 * 8
+    assert w(8, 1, 1, 1) >= 2 * pair + 8 + 8 + 2 * 2 * 64 * 8
+    assert w(64, 1, 1, 1) == w(8, 1, 1, 1)           # padded to 64 either way
+    assert w(64, 3, 1, 10) - w(64, 2, 1, 10) >= pair
+    assert w(64, 1, 2, 10) - w(64, 1, 1, 10) >= pair
+    assert w(64, 1, 1, 4000) > w(64, 1, 1, 10)
+    assert w(64, 1, 1, 10) % 256 == 0
+
+
 def _c_layout(struct_name, fields):
     prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "lime_gb300.h"', 'int main(void){',
             'printf("%zu\\n", sizeof({}));'.format(struct_name)]
