@@ -11,9 +11,13 @@
 // The array is a file-scope __device__ variable, so every GPU on which the
 // library is loaded holds LIME_NOALLOC_SCRATCH_BYTES of it until the process
 // exits.  In host code its name only denotes a host-side stand-in, never a
-// device address; the device address is looked up once per device with
-// cudaGetSymbolAddress, with that device current, on the first call made on
-// that device.
+// device address; the device address is looked up with cudaGetSymbolAddress,
+// with the device current, on the first call in each CUDA context: the cache
+// is keyed on the context's process-unique ID (cuCtxGetId), so a new context
+// on the same device (after cudaDeviceReset, or a context the caller made
+// current) looks the address up again instead of reusing a stale one.
+
+#include <cuda.h>
 
 #include <mutex>
 
@@ -26,21 +30,59 @@ constexpr int kMaxDevices = 64;
 
 __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-std::mutex g_mu;
-void* g_scratch_dev[kMaxDevices] = {nullptr};
+struct Entry {
+  unsigned long long ctx_id;   // context the address belongs to (0: none cached)
+  void* ptr;
+};
 
-// Device address of g_scratch on the current device (set up on first use).
+std::mutex g_mu;
+Entry g_scratch_dev[kMaxDevices] = {};
+
+// ID of the current context, or 0 when none is current.  The two driver
+// calls are fetched through the runtime (cudaGetDriverEntryPointByVersion),
+// so the library needs the driver library only once a GPU is used.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return 0;
+    get_current = reinterpret_cast<GetCurrent>(f1);
+    get_id = reinterpret_cast<GetId>(f2);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Device address of g_scratch in the current context (looked up on the first
+// call in each context).
 int scratch_address(void** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return LIME_ERR_NO_DEVICE;
   if (dev < 0 || dev >= kMaxDevices) return LIME_ERR_UNSUPPORTED;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_dev[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return LIME_ERR_CUDA;
-    g_scratch_dev[dev] = p;
+  unsigned long long id = current_context_id();
+  Entry& e = g_scratch_dev[dev];
+  if (id != 0 && e.ptr && e.ctx_id == id) {
+    *out = e.ptr;
+    return LIME_OK;
   }
-  *out = g_scratch_dev[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return LIME_ERR_CUDA;
+  if (id == 0) id = current_context_id();   // the lookup made the device's context current
+  e.ctx_id = id;
+  e.ptr = id != 0 ? p : nullptr;            // no ID: look it up again next time
+  *out = p;
   return LIME_OK;
 }
 

@@ -92,6 +92,24 @@ def test_noalloc_matches_workspace_entry_point_twice(lib):
         assert relerr(rho, ref_rho) < RTOL
 
 
+def test_noalloc_multi_launch_call_after_a_larger_one(lib):
+    """A 60-step call at n = 64 with two dense operators runs as three
+    launches (about 25 steps each) whose later launches read the start trace
+    the first one left in the scratch array; it follows a call with more
+    instances, so every scratch buffer it uses holds stale data first."""
+    from lime_gb300 import engine
+    H, c_ops, e_ops = _case(64, 4, 2, 21)
+    gen = engine.LindbladGenerator.build(H, c_ops)
+    _run(lib, gen, chains.ground_dm(64), e_ops, 10, noalloc=True)
+    H, c_ops, e_ops = _case(64, 2, 2, 22)
+    gen = engine.LindbladGenerator.build(H, c_ops)
+    rho0 = chains.ground_dm(64)
+    ref_obs, ref_rho = _run(lib, gen, rho0, e_ops, 60, noalloc=False)
+    obs, rho = _run(lib, gen, rho0, e_ops, 60, noalloc=True)
+    assert relerr(obs, ref_obs) < RTOL
+    assert relerr(rho, ref_rho) < RTOL
+
+
 def test_noalloc_rejects_requests_beyond_the_scratch(lib):
     from lime_gb300 import _native as nat
     cap = lib.lime_noalloc_scratch_bytes()
