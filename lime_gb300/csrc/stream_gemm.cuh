@@ -56,6 +56,22 @@ constexpr float kBMax = 8192.f;                    // |B| bound of the 10-bit fi
 constexpr float kMagicB = 1.5f * 8388608.f * 8.f;  // 1.5 * 2^23 * 8: (x + M) - M rounds x to a multiple of 8
 constexpr int kFStride = kBN + 4;                  // padded column of the parked tile (floats)
 
+// The epilogue's index arithmetic holds only for these shapes.  Each column
+// group is drained by four warps (one per TMEM lane quadrant: a warp may
+// only read its own 32 lanes), 16 columns per tcgen05.ld, and the groups
+// must tile the accumulator exactly: a width that over-covers it (three
+// groups of 48 columns for a 12-warp epilogue: 144 > 128) reads TMEM columns
+// past the allocation (D1 of the second buffer at 2*128 + 128 + 96 + 47 =
+// 527 > 511) and writes the two-sum words past S.lo, over the barriers and
+// beyond the dynamic shared allocation: an illegal address.
+static_assert(kEpiWarps % 4 == 0, "a column group needs one warp per TMEM lane quadrant");
+static_assert(kEpiCols % 16 == 0, "the drain reads 16 accumulator columns per tcgen05.ld");
+static_assert(kEpiCols * (kEpiWarps / 4) == kBN, "the column groups must tile the tile's columns exactly");
+static_assert(2 * 2 * kBN <= (int)kTmemCols, "D0 and D1, double-buffered, must fit the TMEM allocation");
+static_assert(kBM == 128, "one accumulator row per TMEM lane");
+static_assert(kThreads <= 1024, "one CTA");
+static_assert(kCK % 16 == 0 && 128 % kCK == 0, "K chunks are whole MMA K steps and divide the exact group");
+
 struct __align__(1024) Smem {
   uint8_t stage[kStages][5][kPiece];               // A0 A1 A2 B0 B1; the parked tile after the last MMA
   float lo[kBN * kBM];                             // low words of the fp32 two-sum accumulators, [col][row]
