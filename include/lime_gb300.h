@@ -56,6 +56,9 @@ typedef enum {
 #define LIME_FLAG_TIMEOUT     0x4  /* a bounded device-side wait expired    */
 #define LIME_FLAG_RANGE       0x8  /* a split-precision operand left its    */
                                    /* fixed-point range (rescale and rerun) */
+#define LIME_FLAG_NOT_HERMITIAN 0x10 /* rho(0) is not Hermitian: the batched */
+                                   /* split kernel's results are invalid;   */
+                                   /* run its two Hermitian parts instead   */
 
 /* ------------------------------------------------------------------ */
 /* Generator preparation                                               */
@@ -370,9 +373,12 @@ int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc* d, void* s
  *     the process exits.  Requests whose workspace
  *     (lime_lindblad_rk4_f64_workspace) exceeds it return
  *     LIME_ERR_SCRATCH_LIMIT without launching anything.
- *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress) with that device current; make that first call
- *     before any stream capture on the device.
+ *   - The first call in each CUDA context looks up the array's device
+ *     address (cudaGetSymbolAddress) with that context's device current;
+ *     make that first call before any stream capture on the device.  A new
+ *     context on the same device (after cudaDeviceReset, or another context
+ *     the caller makes current) is recognised by its ID and looked up again,
+ *     so that first call too belongs before any capture.
  *   - Nothing is allocated or freed by this call.
  *   - All calls in the process share one array per device and it keeps the
  *     previous call's contents; every word a call reads it first writes, but
@@ -433,10 +439,40 @@ typedef struct {
   const double* drive_ops;
   const double* drive_coef;
   void* workspace;        size_t workspace_bytes;
+  /* optional (zero / NULL keeps the behaviour above):
+   * a_pieces      the A operand prepared once per generator by
+   *               lime_lindblad_split_prepare with the same heff and
+   *               scale_a_log2 (undriven calls only); a_stride its bytes per
+   *               parameter set (0 = shared, else 98304)
+   * rho_out       [B][n][n] final state (NULL: written over rho)
+   * auto_scale_b  1: each instance takes its B scale from its own rho(0),
+   *               2^b sqrt(n) ||rho(0)||_F <= 2^13 (scale_b_log2 ignored)
+   * Every instance's rho(0) is checked for Hermiticity on the float pair of
+   * each element; a non-Hermitian one raises LIME_FLAG_NOT_HERMITIAN. */
+  const void* a_pieces;   int64_t a_stride;
+  double* rho_out;
+  int32_t auto_scale_b;
 } LimeLindbladSplitDesc;
 
 size_t lime_lindblad_split_workspace(int32_t n, int32_t param_batch, int32_t n_drive, int32_t n_steps);
 int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream);
+
+/* The A operand of lime_lindblad_rk4_split, split once per generator instead
+ * of once per instance and call (no reference counterpart: it hoists the
+ * per-call operand conversion out of the time loop of lime/oqs.py:1590-1688):
+ * each block row of 2^scale_a_log2 [[Hr, -Hi], [Hi, Hr]] as a per-row 7-bit
+ * fixed-point part + two fp16 residuals, in the order the kernel stores them
+ * to tensor memory.  heff [count][n][n] (stride heff_stride complex elements,
+ * 0 with count 1); out: lime_lindblad_split_prepared_bytes(n, count) bytes,
+ * 16-byte aligned. */
+typedef struct {
+  int32_t n, count, scale_a_log2;
+  const double* heff;     int64_t heff_stride;
+  void* out;              size_t out_bytes;
+} LimeLindbladSplitPrepareDesc;
+
+size_t lime_lindblad_split_prepared_bytes(int32_t n, int32_t count);
+int lime_lindblad_split_prepare(const LimeLindbladSplitPrepareDesc* d, void* stream);
 
 /* ------------------------------------------------------------------ */
 /* Self-test of the bounded device-side waits (test infrastructure)     */

@@ -22,6 +22,7 @@ LIME_FLAG_NONFINITE = 0x1
 LIME_FLAG_TRACE_DRIFT = 0x2
 LIME_FLAG_TIMEOUT = 0x4
 LIME_FLAG_RANGE = 0x8
+LIME_FLAG_NOT_HERMITIAN = 0x10
 
 
 class LimeError(RuntimeError):
@@ -46,6 +47,8 @@ class KernelFlagError(RuntimeError):
             names.append('device-side wait timed out')
         if flags & LIME_FLAG_RANGE:
             names.append('split-precision operand outside its fixed-point range')
+        if flags & LIME_FLAG_NOT_HERMITIAN:
+            names.append('rho(0) is not Hermitian')
         super().__init__('%s: %s (flags 0x%x)' % (where, ', '.join(names) or 'unknown', flags))
 
 
@@ -88,7 +91,16 @@ class SplitDesc(ctypes.Structure):
                 ('n_drive', c_int32),
                 ('drive_ops', c_void_p),
                 ('drive_coef', c_void_p),
-                ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t),
+                ('a_pieces', c_void_p), ('a_stride', c_int64),
+                ('rho_out', c_void_p),
+                ('auto_scale_b', c_int32)]
+
+
+class SplitPrepareDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('count', c_int32), ('scale_a_log2', c_int32),
+                ('heff', c_void_p), ('heff_stride', c_int64),
+                ('out', c_void_p), ('out_bytes', c_size_t)]
 
 
 class AdjointDesc(ctypes.Structure):
@@ -193,6 +205,8 @@ SIGNATURES = [
     ('lime_lindblad_rk4_f64_noalloc', c_int32, [ctypes.POINTER(LindbladDesc), c_void_p]),
     ('lime_lindblad_split_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_split', c_int32, [ctypes.POINTER(SplitDesc), c_void_p]),
+    ('lime_lindblad_split_prepared_bytes', c_size_t, [c_int32, c_int32]),
+    ('lime_lindblad_split_prepare', c_int32, [ctypes.POINTER(SplitPrepareDesc), c_void_p]),
     ('lime_wait_selftest_workspace', c_size_t, []),
     ('lime_wait_selftest', c_int32, [c_int32, ctypes.c_uint32, c_void_p, c_void_p, c_void_p]),
     ('lime_device_check', c_int32, []),

@@ -55,6 +55,7 @@
 // and the results are those of the natural-unit arithmetic scaled exactly.
 
 #include "common.cuh"
+#include "fpconv.cuh"
 #include "tc_ptx.cuh"
 
 namespace lime {
@@ -69,8 +70,13 @@ constexpr uint32_t kColA0 = 0, kColA1 = 64, kColA2 = 128, kColD = 192;
 constexpr uint32_t kLBO = 128;           // B operand: K-direction core-matrix stride (bytes)
 constexpr uint32_t kSBO = 2048;          // B operand: N-direction 8-row-group stride (bytes)
 constexpr uint32_t kBopBytes = 16384;    // 64 (N) x 128 (K) fp16
-constexpr double kA0Max = 127.0;         // |A0| / q_A
 constexpr float kRowFloor = 8.f;         // smallest row bound used for q_B (scaled units)
+// thread (r, h): TMEM lane r of the 128-row block [Xr; Xi], columns [kCols h, kCols h + kCols)
+static_assert(kThreads == 2 * 128 && 2 * kCols == kN, "two column halves of 32 over 128 lanes");
+static_assert(kColA1 == kColA0 + kN && kColA2 == kColA1 + kN && kColD == kColA2 + kN && kColD + kN <= kTmemCols,
+              "three A pieces and the accumulator fit the TMEM allocation");
+static_assert(kBopBytes == kN * 128 * 2, "B operand: 64 columns x 128 K of fp16");
+static_assert(kXtStride >= kN && kXtStride % 4 == 0, "transpose rows hold 64 floats, float4-aligned");
 
 struct __align__(1024) Smem {
   uint8_t bop[2][kBopBytes];             // B0 (fixed point), B1 (residual)
@@ -78,15 +84,24 @@ struct __align__(1024) Smem {
   float rlo[kN * 128];                   // compensation of rho, [j][r]
   float smax[2][kThreads];               // per-thread max |B| of the last written stage input
   double red[2][kThreads / 32];
+  float redf[kThreads / 32];
+  double trp[2];                         // trace partial sums of the two warps owning the diagonal
+  double trs[2];                         // partial traces of rho(0) (the same two warps)
+  double tr0;                            // trace of the instance's rho(0)
+  int eb;                                // the instance's B scale exponent b
   uint64_t mbar;
   uint32_t tmem_base;
 };
+static_assert(offsetof(Smem, xt) == 2 * kBopBytes && 2 * kBopBytes + sizeof(Smem::xt) >= kN * kN * 16,
+              "the B buffers and the transpose buffer, contiguous, hold the staged 64 x 64 complex128 matrix");
 
 struct Args {
   int n, batch, param_batch, n_steps, step0, obs_mode, n_obs, obs_every, obs_per_inst;
-  // sb = 2^b, inv_sb = 2^-b, sa_half = 2^(a-1); the RK4 constants dt/2, dt,
-  // dt/6 (+ its low part) multiplied by 2^-a (accumulator -> B units)
-  float sb, inv_sb, sa_half, c_half, c_full, c_sixth, c_sixth_lo;
+  // eb: the B scale exponent b when auto_b is off; sa_half = 2^(a-1); the
+  // RK4 constants dt/2, dt, dt/6 (+ its low part) multiplied by 2^-a
+  // (accumulator -> B units)
+  int eb;
+  float sa_half, c_half, c_full, c_sixth, c_sixth_lo;
   double sa_d;
   double trace_tol;
   double2* rho;
@@ -108,6 +123,11 @@ struct Args {
   // per (matrix, component, row): first and last nonzero column (x > y: none)
   const int2* heff_rng;
   const int2* drive_rng;
+  // A operand prepared once per generator (prepare_a_kernel), or null
+  const uint4* a_pieces; int64_t a_stride;   // stride in uint4 per parameter set (0: shared)
+  int auto_b;                                // per-instance B scale from ||rho(0)||_F
+  int n_prefetch;                            // instances per CTA whose inputs are prefetched to L2
+  double2* rho_out;                          // final state (may equal rho)
 };
 
 __device__ __forceinline__ double block_sum(double v, double* red, int t) {
@@ -137,16 +157,6 @@ __device__ __forceinline__ uint32_t pack_half2(__half lo, __half hi) {
 __device__ __forceinline__ uint32_t pack_f2h2(float lo, float hi) {
   const __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<const uint32_t*>(&h);
-}
-
-// x = a0 + a1 + a2: a0 on the q grid (|a0| <= 127 q), a1/a2 fp16 residuals.
-__device__ __forceinline__ void split_a(double x, double q, double inv_q, __half& a0, __half& a1, __half& a2) {
-  const double k = fmin(fmax(rint(x * inv_q), -kA0Max), kA0Max);
-  const double v0 = k * q;
-  a0 = __double2half(v0);
-  const double r1 = x - v0;
-  a1 = __double2half(r1);
-  a2 = __double2half(r1 - (double)__half2float(a1));
 }
 
 // Row quantum from a bound m of |B| on the row (scaled units): |x| <= 1.5 m
@@ -197,6 +207,91 @@ __device__ __forceinline__ void split_a32(float xh, float xl, float magic, float
   a0 = __float2half_rn(v0);
   a1 = __float2half_rn(r);
   a2 = __float2half_rn(__fsub_rn(r, __half2float(a1)));
+}
+
+// Quantum of a block row of A from its bound rmax (scaled units): magic
+// rounds to multiples of q = 2^(ilogb(rmax) - 6) and qmax = 127 q clamps
+// A0; a row below 2^-18 gets no fixed-point part (magic rounds to integers,
+// qmax = 0).
+__device__ __forceinline__ void a_row_quantum(float rmax, float& magic, float& qmax) {
+  if (rmax >= 0x1p-18f) {
+    const int e = ilogbf(rmax);
+    magic = ldexpf(1.5f, e - 6 + 23);
+    qmax = ldexpf(127.f, e - 6);
+  } else {
+    magic = 12582912.f;   // 1.5 * 2^23
+    qmax = 0.f;
+  }
+}
+
+// max |A| over the 128 entries of block row (i, component) of 2^a Heff.
+__device__ __forceinline__ float a_row_max(const double2* heff, int n, int i, bool xi_row, double sa) {
+  float m = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < 128; ++k) m = fmaxf(m, fabsf((float)(a_elem(heff, n, i, k, xi_row) * sa)));
+  return m;
+}
+
+// The A pieces of block row (i, component) for k in [64 h + 32 qq, + 32),
+// two halves to a word.  Each entry x = 2^a h (exact in FP64) becomes the
+// float pair (float) x + (float)(x - (float) x) (~48 bits), split by
+// split_a32: three FP64 operations an entry, FP64 being slow on this part.
+__device__ __forceinline__ void a_pieces_row(const double2* heff, int n, int i, bool xi_row, int h, int qq, double sa,
+                                             float magic, float qmax, uint32_t (&p0)[16], uint32_t (&p1)[16],
+                                             uint32_t (&p2)[16]) {
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const int k = 64 * h + 32 * qq + 2 * c;
+    __half x0, x1, x2, y0, y1, y2;
+    const double u = a_elem(heff, n, i, k, xi_row) * sa;
+    const double w = a_elem(heff, n, i, k + 1, xi_row) * sa;
+    const float uh = (float)u, wh = (float)w;
+    split_a32(uh, (float)(u - (double)uh), magic, qmax, x0, x1, x2);
+    split_a32(wh, (float)(w - (double)wh), magic, qmax, y0, y1, y2);
+    p0[c] = pack_half2(x0, y0);
+    p1[c] = pack_half2(x1, y1);
+    p2[c] = pack_half2(x2, y2);
+  }
+}
+
+// Prepared A operand of one generator: uint4 words in the order
+// [piece 3][qq 2][h 2][c4 4][row 128], i.e. the 16 words thread (row, h)
+// stores to TMEM columns [32 h + 16 qq, + 16) of piece `piece` are the
+// four uint4 at c4 = 0..3, and a warp's 32 rows read 512 contiguous bytes.
+constexpr int kAPieceU4 = 3 * 2 * 2 * 4 * 128;    // 98304 bytes per generator
+__host__ __device__ __forceinline__ int a_piece_index(int piece, int qq, int h, int c4, int row) {
+  return (((piece * 2 + qq) * 2 + h) * 4 + c4) * 128 + row;
+}
+
+// Position of element (i, j) of the 64 x 64 double2 matrix staged in shared
+// memory: rows of 64, columns XOR-permuted within aligned groups of 8 by
+// i & 7, so that a warp's 32 rows at one column (the per-thread component
+// reads and writes) spread over 8 bank groups, while 8 consecutive columns
+// of a row (the coalesced copies) stay one contiguous 128-byte run.
+__device__ __forceinline__ int stage_index(int i, int j) { return i * kN + (j ^ (i & 7)); }
+
+// One CTA per generator, the thread layout of the propagation kernel.
+__global__ void __launch_bounds__(kThreads) prepare_a_kernel(const double2* heff, int64_t heff_stride, int n,
+                                                              double sa, uint4* out) {
+  const int t = threadIdx.x, warp = t >> 5;
+  const int r = (warp & 3) * 32 + (t & 31), h = warp >> 2;
+  const bool xi_row = r >= 64;
+  const int i = r & 63;
+  const double2* H = heff + (int64_t)blockIdx.x * heff_stride;
+  uint4* o = out + (int64_t)blockIdx.x * kAPieceU4;
+  float magic, qmax;
+  a_row_quantum(a_row_max(H, n, i, xi_row, sa), magic, qmax);
+#pragma unroll 1
+  for (int qq = 0; qq < 2; ++qq) {
+    uint32_t p[3][16];
+    a_pieces_row(H, n, i, xi_row, h, qq, sa, magic, qmax, p[0], p[1], p[2]);
+#pragma unroll
+    for (int piece = 0; piece < 3; ++piece)
+#pragma unroll
+      for (int c4 = 0; c4 < 4; ++c4)
+        o[a_piece_index(piece, qq, h, c4, r)] =
+            make_uint4(p[piece][4 * c4], p[piece][4 * c4 + 1], p[piece][4 * c4 + 2], p[piece][4 * c4 + 3]);
+  }
 }
 
 // Issue one MMA pass (thread 0) and commit it to mbar; every thread then
@@ -260,7 +355,6 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
   const uint64_t desc_b1 = tc::smem_desc_noswizzle(tc::smem_u32(S.bop[1]), kLBO, kSBO);
   const uint32_t brow = (uint32_t)(i >> 3) * kSBO + (uint32_t)(i & 7) * 16u;
   const uint32_t bchunk0 = (is_re ? 0u : 8u) + 4u * (uint32_t)h;
-  const float bsign = is_re ? a.sb : -a.sb;   // natural -> B units of this thread's component
   const float tsign = is_re ? 1.f : -1.f;      // u = own +- transposed element
   float* xrow = S.xt + r * kXtStride;
   const float* xcol = S.xt + (is_re ? 64 : 0) * kXtStride + i;   // X[j][i] at xcol[j * stride]
@@ -274,6 +368,17 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
     const double2* heff = a.heff + p * a.heff_stride;
     const float mi = (a.m_diag && i < n) ? (float)a.m_diag[p * a.m_stride + i] : 0.f;
 
+    // inputs of this CTA's next instance into L2 while this one runs
+    if (t == 0 && b + (int)gridDim.x < a.batch) {
+      const int bn = b + (int)gridDim.x;
+      tc::bulk_prefetch_l2(a.rho + (int64_t)bn * n * n, (uint32_t)(n * n * 16));
+      if (!kDrive && a.a_pieces && a.a_stride) {
+        const uint4* an = a.a_pieces + (int64_t)(bn % a.param_batch) * a.a_stride;
+        tc::bulk_prefetch_l2(an, kAPieceU4 * 8u);
+        tc::bulk_prefetch_l2(an + kAPieceU4 / 2, kAPieceU4 * 8u);
+      }
+    }
+
     // ---- driven: the row's quantum from its bound over the whole drive; the
     // A pieces are written at the start of every step ----
     float magic_a = 0.f, qmax_a = 0.f;
@@ -285,70 +390,136 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         for (int k = 0; k < 128; ++k) mr = fmax(mr, fabs(a_elem(a.drive_ops + (int64_t)dd * n * n, n, i, k, is_re)));
         rmax += a.coef_max[dd] * mr;
       }
-      rmax *= a.sa_d;
-      if (rmax >= 0x1p-18) {
-        const int e = ilogb(rmax);
-        magic_a = ldexpf(1.5f, e - 6 + 23);
-        qmax_a = ldexpf(127.f, e - 6);
-      } else {
-        magic_a = 12582912.f;   // 1.5 * 2^23: rounds to integers, then clamped to 0
-      }
+      a_row_quantum((float)(rmax * a.sa_d), magic_a, qmax_a);
     }
-    // ---- A operand: scaled Heff block row r -> TMEM as A0 + A1 + A2 (this thread: k in [64h, 64h+64)) ----
+    // ---- A operand: block row r of 2^a Heff -> TMEM as A0 + A1 + A2 (this
+    // thread: k in [64h, 64h+64)), from the prepared pieces or split here ----
     if (!kDrive) {
-      double rmax = 0.0;
-      for (int k = 0; k < 128; ++k) rmax = fmax(rmax, fabs(a_elem(heff, n, i, k, is_re) * a.sa_d));
-      double q = 1.0, inv_q = 0.0;   // inv_q = 0: no fixed-point part for negligible rows
-      if (rmax >= 0x1p-18) {
-        const int e = ilogb(rmax);
-        q = ldexp(1.0, e - 6);
-        inv_q = ldexp(1.0, 6 - e);
-      }
-#pragma unroll 1
-      for (int qq = 0; qq < 2; ++qq) {
-        uint32_t p0[16], p1[16], p2[16];
+      float magic = 0.f, qmax = 0.f;
+      if (!a.a_pieces) a_row_quantum(a_row_max(heff, n, i, is_re, a.sa_d), magic, qmax);
+      if (a.a_pieces) {
+        // all 24 loads in flight before the tensor-memory stores
+        const uint4* src = a.a_pieces + (int64_t)p * a.a_stride;
+        uint4 v[3][2][4];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const int k = 64 * h + qq * 32 + 2 * c;
-          __half x0, x1, x2, y0, y1, y2;
-          split_a(a_elem(heff, n, i, k, is_re) * a.sa_d, q, inv_q, x0, x1, x2);
-          split_a(a_elem(heff, n, i, k + 1, is_re) * a.sa_d, q, inv_q, y0, y1, y2);
-          p0[c] = pack_half2(x0, y0);
-          p1[c] = pack_half2(x1, y1);
-          p2[c] = pack_half2(x2, y2);
+        for (int piece = 0; piece < 3; ++piece)
+#pragma unroll
+          for (int qq = 0; qq < 2; ++qq)
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) v[piece][qq][c4] = src[a_piece_index(piece, qq, h, c4, r)];
+#pragma unroll
+        for (int piece = 0; piece < 3; ++piece)
+#pragma unroll
+          for (int qq = 0; qq < 2; ++qq) {
+            uint32_t w[16];
+#pragma unroll
+            for (int c4 = 0; c4 < 4; ++c4) {
+              w[4 * c4] = v[piece][qq][c4].x;
+              w[4 * c4 + 1] = v[piece][qq][c4].y;
+              w[4 * c4 + 2] = v[piece][qq][c4].z;
+              w[4 * c4 + 3] = v[piece][qq][c4].w;
+            }
+            tc::tmem_st16(lane_addr + kColA0 + 64u * piece + 32 * h + 16 * qq, w);
+          }
+      } else {
+#pragma unroll 1
+        for (int qq = 0; qq < 2; ++qq) {
+          uint32_t p0[16], p1[16], p2[16];
+          a_pieces_row(heff, n, i, is_re, h, qq, a.sa_d, magic, qmax, p0, p1, p2);
+          const uint32_t col = 32 * h + 16 * qq;
+          tc::tmem_st16(lane_addr + kColA0 + col, p0);
+          tc::tmem_st16(lane_addr + kColA1 + col, p1);
+          tc::tmem_st16(lane_addr + kColA2 + col, p2);
         }
-        const uint32_t col = 32 * h + 16 * qq;
-        tc::tmem_st16(lane_addr + kColA0 + col, p0);
-        tc::tmem_st16(lane_addr + kColA1 + col, p1);
-        tc::tmem_st16(lane_addr + kColA2 + col, p2);
       }
       tc::tmem_wait_st();
     }
 
-    // ---- state: columns [j0, j0+32) of this thread's row component, B units ----
+    // ---- state: rho(0) is staged through shared memory (the idle B operand
+    // and transpose buffers, 64 KB) as a 64 x 64 double2 matrix, loaded with
+    // coalesced 16-byte loads; each thread then reads its row component
+    // (columns [j0, j0+32)) and, for the Hermiticity check, the transposed
+    // element.  Element (i, j) sits at stage_index(i, j).
+    double2* stg = reinterpret_cast<double2*>(S.bop[0]);
+    {
+      const double2* r0 = a.rho + (int64_t)b * n * n;
+#pragma unroll 4
+      for (int e = t; e < kN * kN; e += kThreads) {
+        const int ii = e >> 6, jj = e & 63;
+        double2 z = make_double2(0.0, 0.0);
+        if (ii < n && jj < n) z = r0[ii * n + jj];
+        stg[stage_index(ii, jj)] = z;
+      }
+    }
+    __syncthreads();
     float rho[kCols], acc[kCols];
-    const double2* r0 = a.rho + (int64_t)b * n * n;
     double dtr = 0.0;
+    float fro = 0.f;
+    bool herm = true;   // rho_ji = conj rho_ij, compared bit for bit (+0 == -0)
+    {
+      const double* sd = reinterpret_cast<const double*>(stg);
+      const int comp = is_re ? 0 : 1;
+      const uint64_t flip = is_re ? 0ull : 0x8000000000000000ull;
+#pragma unroll
+      for (int jj = 0; jj < kCols; ++jj) {
+        const int j = j0 + jj;
+        const double v = sd[2 * stage_index(i, j) + comp];
+        const uint64_t bv = fpconv::bits64(v);
+        const uint64_t bw = fpconv::bits64(sd[2 * stage_index(j, i) + comp]) ^ flip;
+        herm &= (bv == bw) || ((bv | bw) << 1) == 0;
+        float hv, lv;
+        fpconv::split_f64(v, hv, lv);   // (float) v and (float)(v - hv) without FP64 instructions
+        rho[jj] = hv;
+        acc[jj] = 0.f;
+        S.rlo[j * 128 + r] = lv;
+        fro = __fmaf_rn(hv, hv, fro);
+        if (diag_owner && j == i) dtr = v;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fro += __shfl_xor_sync(0xffffffffu, fro, o);
+    if (warp == 2 || warp == 7) {   // the warps that own the diagonal
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) dtr += __shfl_xor_sync(0xffffffffu, dtr, o);
+      if ((t & 31) == 0) S.trs[warp == 7 ? 1 : 0] = dtr;
+    }
+    if ((t & 31) == 0) S.redf[warp] = fro;
+    __syncthreads();   // (also: every read of the staged matrix is done)
+    float fro_all = 0.f;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) fro_all += S.redf[w];
+    // B scale: 2^b sqrt(n) ||rho||_F <= 2^13 (sqrt(n) ||rho||_F bounds every
+    // |rho_ij(t)|: the trace norm contracts), per instance when auto_b
+    int eb = a.eb;
+    if (a.auto_b) {
+      const float bound = sqrtf((float)n * fro_all);
+      eb = 0;
+      if (bound > 0.f && isfinite(bound)) {
+        const int e = ilogbf(bound);
+        eb = (bound == ldexpf(1.f, e)) ? 13 - e : 12 - e;
+        eb = max(-60, min(60, eb));
+      }
+    }
+    const float sbi = ldexpf(1.f, eb);
+    const float bsign = is_re ? sbi : -sbi;   // natural -> B units of this thread's component
     float mx = 0.f;
     float rho_d = 0.f, acc_d = 0.f, rs_d = 0.f;   // diagonal element (diag_owner only)
 #pragma unroll
     for (int jj = 0; jj < kCols; ++jj) {
       const int j = j0 + jj;
-      double v = 0.0;
-      if (i < n && j < n) {
-        const double2 z = r0[(int64_t)i * n + j];
-        v = is_re ? z.x : z.y;
-      }
-      const float hv = (float)v;
-      rho[jj] = hv * bsign;
-      acc[jj] = 0.f;
-      S.rlo[j * 128 + r] = (float)(v - (double)hv) * bsign;
+      rho[jj] *= bsign;
+      S.rlo[j * 128 + r] *= bsign;
       mx = fmaxf(mx, fabsf(rho[jj]));
-      if (diag_owner && j == i) { dtr = v; rho_d = rho[jj]; }
+      if (diag_owner && j == i) rho_d = rho[jj];
     }
+    if (!herm) flags |= LIME_FLAG_NOT_HERMITIAN;
     rs_d = rho_d;
     S.smax[g & 1][t] = mx;
-    const double tr0 = block_sum(dtr, S.red[0], t);   // (its barriers publish smax)
+    if (t == 0) {   // read after the barriers below (kept out of the step loop's registers)
+      S.tr0 = S.trs[0] + S.trs[1];
+      S.eb = eb;
+    }
+    __syncthreads();   // publishes smax
     {
       const float m4 = fmaxf(fmaxf(S.smax[g & 1][i], S.smax[g & 1][64 + i]),
                              fmaxf(S.smax[g & 1][128 + i], S.smax[g & 1][192 + i]));
@@ -362,6 +533,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         store_b8(S, brow + (bchunk0 + c) * kLBO, x, magic, dummy);
       }
     }
+    bool tr_pending = false;   // a trace recorded after the last step awaits its check
 
 #pragma unroll 1
     for (int step = 0; step < a.n_steps; ++step) {
@@ -418,6 +590,11 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
         tc::tc_fence_before();
         __syncthreads();
         if (t == 0) mma_pass<false>(tbase, desc_b0, desc_b1, &S.mbar);
+        if (tr_pending) {
+          if (t == 0 && fabs(S.trp[0] + S.trp[1] - S.tr0) > a.trace_tol * fmax(1.0, fabs(S.tr0)))
+            flags |= LIME_FLAG_TRACE_DRIFT;
+          tr_pending = false;
+        }
         int timed_out = tc::mbar_wait_bounded(&S.mbar, phase, a.max_wait) ? 0 : 1;
         phase ^= 1u;
         tc::tc_fence_after();
@@ -527,7 +704,9 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       if (((gstep + 1) % a.obs_every) == 0) {
         const int slot = (gstep + 1) / a.obs_every - 1;
         double2* orow = a.obs_out + ((int64_t)b * a.obs_per_inst + slot) * a.n_obs;
-        const double dval = diag_owner ? ((double)rho_d + (double)S.rlo[i * 128 + r]) * (double)a.inv_sb : 0.0;
+        const double dval =
+            diag_owner ? fpconv::scale_pow2(fpconv::widen_f32(rho_d) + fpconv::widen_f32(S.rlo[i * 128 + r]), -S.eb)
+                       : 0.0;
         if (a.obs_mode == 1) {
           if (diag_owner && i < a.n_obs) orow[i] = make_double2(dval, 0.0);
         } else if (a.obs_mode == 2) {
@@ -553,34 +732,55 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
                 }
               }
             }
-            const double sr = block_sum((double)pr, S.red[0], t) * (double)a.inv_sb;
-            const double si = block_sum((double)pi, S.red[1], t) * (double)a.inv_sb;
+            const double sr = fpconv::scale_pow2(block_sum((double)pr, S.red[0], t), -S.eb);
+            const double si = fpconv::scale_pow2(block_sum((double)pi, S.red[1], t), -S.eb);
             if (t == 0) orow[o] = make_double2(sr, si);
           }
         }
         if (a.trace_tol > 0.0) {
-          const double tr = block_sum((diag_owner && i < n) ? dval : 0.0, S.red[0], t);
-          if (fabs(tr - tr0) > a.trace_tol * fmax(1.0, fabs(tr0))) flags |= LIME_FLAG_TRACE_DRIFT;
+          // the diagonal lives in warps 2 (i < 32) and 7 (i >= 32); their sums
+          // are compared with tr0 by thread 0 after the next barrier
+          if (warp == 2 || warp == 7) {
+            double v = (diag_owner && i < n) ? dval : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((t & 31) == 0) S.trp[warp == 7 ? 1 : 0] = v;
+          }
+          tr_pending = true;
         }
       }
     }
     if (aborted) break;
 
-    // ---- final state: rho = hi + lo in FP64 ----
-    if (i < n) {
-      double* out = reinterpret_cast<double*>(a.rho + (int64_t)b * n * n);
-      const double to_nat = is_re ? (double)a.inv_sb : -(double)a.inv_sb;
+    // ---- final state: hi + lo of every element into the staged matrix
+    // (one FP64 addition each; widening, power-of-two scale and sign without
+    // FP64 instructions), then coalesced 16-byte stores ----
+    __syncthreads();   // the last stage's reads of the transpose buffer are done
+    {
+      double* sd = reinterpret_cast<double*>(stg);
+      const int comp = is_re ? 0 : 1;
+      const int ebi = -S.eb;
+      const uint64_t neg = is_re ? 0ull : 0x8000000000000000ull;   // B units hold -2^b Im rho
 #pragma unroll
       for (int jj = 0; jj < kCols; ++jj) {
         const int j = j0 + jj;
-        if (j < n) {
-          const double v = ((double)rho[jj] + (double)S.rlo[j * 128 + r]) * to_nat;
-          if (!isfinite(v)) flags |= LIME_FLAG_NONFINITE;
-          out[2 * ((int64_t)i * n + j) + (is_re ? 0 : 1)] = v;
-        }
+        const double v = fpconv::scale_pow2(fpconv::widen_f32(rho[jj]) + fpconv::widen_f32(S.rlo[j * 128 + r]), ebi);
+        if (!isfinite(rho[jj])) flags |= LIME_FLAG_NONFINITE;
+        sd[2 * stage_index(i, j) + comp] = fpconv::from_bits64(fpconv::bits64(v) ^ neg);
+      }
+    }
+    __syncthreads();
+    {
+      double2* out = a.rho_out + (int64_t)b * n * n;
+#pragma unroll 4
+      for (int e = t; e < n * n; e += kThreads) {
+        const int ii = e / n, jj = e - ii * n;
+        out[e] = stg[stage_index(ii, jj)];
       }
     }
     __syncthreads();   // smax / rlo of this instance are no longer read
+    if (tr_pending && t == 0 && fabs(S.trp[0] + S.trp[1] - S.tr0) > a.trace_tol * fmax(1.0, fabs(S.tr0)))
+      flags |= LIME_FLAG_TRACE_DRIFT;
   }
 
   if (aborted) {
@@ -682,6 +882,28 @@ extern "C" size_t lime_lindblad_split_workspace(int32_t n, int32_t param_batch, 
   return split::drive_ws(param_batch, n_drive, n_steps).total;
 }
 
+extern "C" size_t lime_lindblad_split_prepared_bytes(int32_t n, int32_t count) {
+  if (n <= 0 || n > split::kN || count <= 0) return 0;
+  return (size_t)count * split::kAPieceU4 * sizeof(uint4);
+}
+
+extern "C" int lime_lindblad_split_prepare(const LimeLindbladSplitPrepareDesc* d, void* stream) {
+  if (!d) return LIME_ERR_ARG;
+  if (d->n <= 0 || d->count <= 0 || !d->heff || !d->out) return LIME_ERR_ARG;
+  if (d->n > split::kN) return LIME_ERR_UNSUPPORTED;
+  if (d->heff_stride < 0 || (d->count > 1 && d->heff_stride < (int64_t)d->n * d->n)) return LIME_ERR_ARG;
+  if (d->scale_a_log2 < -60 || d->scale_a_log2 > 60) return LIME_ERR_ARG;
+  if ((reinterpret_cast<uintptr_t>(d->heff) & 15) != 0 || (reinterpret_cast<uintptr_t>(d->out) & 15) != 0)
+    return LIME_ERR_ARG;
+  if (d->out_bytes < lime_lindblad_split_prepared_bytes(d->n, d->count)) return LIME_ERR_WORKSPACE;
+  split::prepare_a_kernel<<<d->count, split::kThreads, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<const double2*>(d->heff), d->heff_stride, d->n, ldexp(1.0, d->scale_a_log2),
+      reinterpret_cast<uint4*>(d->out));
+  LIME_CUDA_TRY(cudaGetLastError());
+  count_launch();
+  return LIME_OK;
+}
+
 extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream) {
   if (!d) return LIME_ERR_ARG;
   if (d->n <= 0 || d->batch <= 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
@@ -704,6 +926,14 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
     if (d->workspace_bytes < lime_lindblad_split_workspace(d->n, pb, d->n_drive, d->n_steps))
       return LIME_ERR_WORKSPACE;
   }
+  if (d->a_pieces) {
+    if (d->n_drive > 0) return LIME_ERR_ARG;   // a driven A is split on the device every step
+    if ((reinterpret_cast<uintptr_t>(d->a_pieces) & 15) != 0) return LIME_ERR_ARG;
+    if (d->a_stride != 0 && d->a_stride != (int64_t)split::kAPieceU4 * 16) return LIME_ERR_ARG;
+  }
+  if ((reinterpret_cast<uintptr_t>(d->rho) & 15) != 0 || (reinterpret_cast<uintptr_t>(d->heff) & 15) != 0 ||
+      (reinterpret_cast<uintptr_t>(d->rho_out) & 15) != 0)
+    return LIME_ERR_ARG;
   if (d->n_steps == 0) return LIME_OK;
   if (g_num_sms == 0) {
     int dev = 0;
@@ -717,8 +947,7 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   a.obs_every = d->obs_every > 0 ? d->obs_every : 1;
   a.obs_per_inst = d->n_steps / a.obs_every;
   a.sa_d = ldexp(1.0, d->scale_a_log2);
-  a.sb = ldexpf(1.f, d->scale_b_log2);
-  a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
+  a.eb = d->scale_b_log2;
   a.sa_half = ldexpf(1.f, d->scale_a_log2 - 1);
   {
     // the fp32 constants of the natural-unit update, then scaled by 2^-a (exact)
@@ -737,6 +966,10 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   a.obs_out = reinterpret_cast<double2*>(d->obs_out);
   a.status = d->status;
   a.max_wait = 1u << 26;
+  a.a_pieces = reinterpret_cast<const uint4*>(d->a_pieces);
+  a.a_stride = d->a_stride / 16;
+  a.auto_b = d->auto_scale_b != 0;
+  a.rho_out = reinterpret_cast<double2*>(d->rho_out ? d->rho_out : d->rho);
   cudaStream_t st = (cudaStream_t)stream;
   const bool driven = d->n_drive > 0;
   if (driven) {

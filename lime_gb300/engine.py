@@ -10,7 +10,7 @@ used only as device buffers whose ``data_ptr()`` is handed to the kernels.
 """
 from __future__ import annotations
 
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 
 import numpy as np
 import torch
@@ -62,6 +62,56 @@ class DiagonalOps:
         self.l = l
 
 
+class SiteDephasing:
+    """Pure site dephasing given by its rates: the n collapse operators
+    sqrt(rates[k]) |k><k|, k = 0 .. n-1.  ``rates`` has shape (n,) (shared)
+    or (P, n) (one set per instance).  Equivalent to
+    ``DiagonalOps(diag_embed(sqrt(rates)))``, with n values per instance
+    passed instead of n^2."""
+
+    def __init__(self, rates):
+        self.rates = rates
+
+    def diagonal_ops(self, device) -> DiagonalOps:
+        g = self.rates
+        g = g.to(device=device, dtype=torch.float64) if isinstance(g, torch.Tensor) else \
+            torch.as_tensor(np.asarray(g, dtype=np.float64), device=device)
+        if g.dim() not in (1, 2):
+            raise ValueError('SiteDephasing rates must be (n,) or (P, n)')
+        return DiagonalOps(torch.diag_embed(torch.sqrt(g)).to(CDT))
+
+
+class Populations:
+    """Observables given compactly: the populations rho_kk of sites
+    k = 0 .. count-1, i.e. the projectors |k><k| as e_ops.  Equivalent to
+    passing those dense projectors (which are recognised too), without
+    building or inspecting count n x n matrices per call."""
+
+    def __init__(self, count: int):
+        self.count = int(count)
+
+    def __len__(self):
+        return self.count
+
+    def dense(self, n: int) -> list:
+        out = []
+        for k in range(self.count):
+            e = np.zeros((n, n), dtype=np.complex128)
+            e[k, k] = 1.0
+            out.append(e)
+        return out
+
+
+def expand_e_ops(e_ops, n: int):
+    """e_ops as a list of operators (a Populations object becomes its dense
+    projectors)."""
+    if isinstance(e_ops, Populations):
+        if e_ops.count > n:
+            raise ValueError('%d populations of a %d-dimensional system' % (e_ops.count, n))
+        return e_ops.dense(n)
+    return e_ops
+
+
 def is_diagonal(op: torch.Tensor) -> bool:
     n = op.shape[-1]
     off = op * (1 - torch.eye(n, dtype=op.dtype, device=op.device))
@@ -78,6 +128,8 @@ class LindbladGenerator:
     l_dense: torch.Tensor | None  # (P|1, K, n, n) or None
     k_dense: int
     shared: bool                  # one generator for every instance
+    # operands of the batched split kernel, built on first use (split_operands)
+    split_cache: dict = field(default_factory=dict, repr=False, compare=False)
 
     @staticmethod
     def build(H, c_ops=None, device=None) -> 'LindbladGenerator':
@@ -94,7 +146,7 @@ class LindbladGenerator:
         if Hd.dim() != 3 or Hd.shape[-1] != Hd.shape[-2]:
             raise ValueError('H must be (n, n) or (P, n, n); got %s' % (tuple(Hd.shape),))
         n = Hd.shape[-1]
-        c_ops = list(c_ops or [])
+        c_ops = [c.diagonal_ops(device) if isinstance(c, SiteDephasing) else c for c in (c_ops or [])]
         packed = [as_device(c.l, device) for c in c_ops if isinstance(c, DiagonalOps)]
         ops = [as_device(c, device) for c in c_ops if not isinstance(c, DiagonalOps)]
         P = Hd.shape[0]
@@ -161,6 +213,15 @@ def hermitian_parts(rho: torch.Tensor):
 
 def prepare_obs(e_ops, n, P, device):
     """Stack observables: returns (tensor, n_obs, obs_diag, stride)."""
+    if isinstance(e_ops, Populations):
+        if e_ops.count > n:
+            raise ValueError('%d populations of a %d-dimensional system' % (e_ops.count, n))
+        if not e_ops.count:
+            return None, 0, 0, 0
+        Et = torch.zeros((1, e_ops.count, n), dtype=CDT, device=device)
+        idx = torch.arange(e_ops.count, device=device)
+        Et[0, idx, idx] = 1
+        return Et, e_ops.count, 1, 0
     if not e_ops:
         return None, 0, 0, 0
     E = [as_device(e, device) for e in e_ops]
@@ -227,14 +288,19 @@ SPLIT_MAX_N = 64
 
 
 def split_supported(gen: LindbladGenerator) -> str | None:
-    """None if the tensor-core path handles ``gen``, else the reason it does not."""
-    if gen.n > SPLIT_MAX_N:
-        return 'dimension %d > %d' % (gen.n, SPLIT_MAX_N)
-    if gen.k_dense:
-        return 'dense (non-diagonal) collapse operators'
-    if gen.m is not None and not is_diagonal(gen.m):
-        return 'diagonal collapse operators with a non-diagonal M = sum_k l_k l_k^dag'
-    return None
+    """None if the batched tensor-core kernel handles ``gen``, else the
+    reason it does not (decided once per generator)."""
+    c = gen.split_cache
+    if 'why' not in c:
+        why = None
+        if gen.n > SPLIT_MAX_N:
+            why = 'dimension %d > %d' % (gen.n, SPLIT_MAX_N)
+        elif gen.k_dense:
+            why = 'dense (non-diagonal) collapse operators'
+        elif gen.m is not None and not is_diagonal(gen.m):
+            why = 'diagonal collapse operators with a non-diagonal M = sum_k l_k l_k^dag'
+        c['why'] = why
+    return c['why']
 
 
 def _pow2_exponent(target: float, bound: float) -> int:
@@ -244,17 +310,76 @@ def _pow2_exponent(target: float, bound: float) -> int:
     return int(math.floor(math.log2(target / bound)))
 
 
+def heff_amax(gen: LindbladGenerator) -> float:
+    """max |Heff| over every generator (computed once per generator)."""
+    c = gen.split_cache
+    if 'amax' not in c:
+        c['amax'] = float(gen.heff.abs().max().item())
+    return c['amax']
+
+
+def split_operands(gen: LindbladGenerator) -> dict:
+    """Operands of the batched split kernel, built once per generator: the A
+    operand (``lime_lindblad_split_prepare``: 2^a Heff in its fixed-point +
+    two fp16 pieces, in the kernel's tensor-memory order), its scale exponent
+    a (max |2^a Heff| in [2^12, 2^13)) and the real diagonal of M."""
+    c = gen.split_cache
+    if 'pieces' not in c:
+        lib = nat.require_device()
+        sa = _pow2_exponent(4096.0, heff_amax(gen))
+        count = gen.heff.shape[0]
+        nbytes = int(lib.lime_lindblad_split_prepared_bytes(gen.n, count))
+        pieces = torch.empty(nbytes, dtype=torch.uint8, device=gen.heff.device)
+        d = nat.SplitPrepareDesc()
+        d.n, d.count, d.scale_a_log2 = gen.n, count, sa
+        d.heff, d.heff_stride = gen.heff.data_ptr(), (gen.n * gen.n if count > 1 else 0)
+        d.out, d.out_bytes = pieces.data_ptr(), nbytes
+        nat.check(lib.lime_lindblad_split_prepare(d, _stream_ptr()), 'lime_lindblad_split_prepare')
+        c['pieces'], c['stride'], c['scale_a'] = pieces, (nbytes // count if count > 1 else 0), sa
+    split_operands_mdiag(gen)
+    return c
+
+
+def _host_array(a):
+    """NumPy view of a host operand, or None for a device tensor."""
+    if isinstance(a, torch.Tensor):
+        return a.detach().resolve_conj().numpy() if a.device.type == 'cpu' else None
+    return _to_dense_np(a)
+
+
+def _is_population(e, k, n) -> bool:
+    """e == |k><k| (n x n), checked on the host."""
+    if e is None or e.shape != (n, n) or e[k, k] != 1:
+        return False
+    return int(np.count_nonzero(e)) == 1
+
+
 def _split_obs(e_ops, n, P, device):
-    """(mode, n_obs, tensor, stride) for the split kernel."""
+    """(mode, n_obs, tensor, stride) for the split kernel.  Site
+    populations given as host arrays are recognised on the host (no device
+    round trip); device tensors are compared on the device."""
+    if isinstance(e_ops, Populations):
+        if e_ops.count > n:
+            raise ValueError('%d populations of a %d-dimensional system' % (e_ops.count, n))
+        return (1, e_ops.count, None, 0) if e_ops.count else (0, 0, None, 0)
     if not e_ops:
         return 0, 0, None, 0
-    E = [as_device(e, device) for e in e_ops]
-    if all(e.dim() == 2 for e in E) and len(E) <= n:
-        pops = torch.zeros((len(E), n, n), dtype=CDT, device=device)
-        idx = torch.arange(len(E), device=device)
-        pops[idx, idx, idx] = 1
-        if torch.equal(torch.stack(E), pops):
-            return 1, len(E), None, 0
+    if len(e_ops) <= n:
+        host = [_host_array(e) for e in e_ops]
+        if all(h is not None for h in host):
+            if all(_is_population(h, k, n) for k, h in enumerate(host)):
+                return 1, len(e_ops), None, 0
+            E = [torch.as_tensor(h, dtype=CDT, device=device) for h in host]
+        else:
+            E = [as_device(e, device) for e in e_ops]
+            if all(e.dim() == 2 for e in E):
+                pops = torch.zeros((len(E), n, n), dtype=CDT, device=device)
+                idx = torch.arange(len(E), device=device)
+                pops[idx, idx, idx] = 1
+                if torch.equal(torch.stack(E), pops):
+                    return 1, len(E), None, 0
+    else:
+        E = [as_device(e, device) for e in e_ops]
     per = any(e.dim() == 3 for e in E)
     if per:
         Et = torch.stack([e.expand(P, n, n) if e.dim() == 2 else e for e in E], 1).contiguous()
@@ -264,41 +389,50 @@ def _split_obs(e_ops, n, P, device):
 
 def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
                obs_every: int, trace_tol: float, param_batch: int, events=None,
-               ctas_per_sm: int = 0, drive=None):
+               ctas_per_sm: int = 0, drive=None, rho_out=None):
     """The batched tensor-core kernel (n <= 64, diagonal collapse operators).
-    State scale: sqrt(n) ||rho(0)||_F (a bound of |rho_ij(t)|: the trace
-    norm contracts) at 2^13; the kernel picks each B row's fixed-point
-    quantum from the previous stage's row bound.  ``drive`` = (ops
-    (n_drive, n, n), coef (n_steps, n_drive)): Heff(t) = Heff - sum_d
-    coef[k, d] ops[d], re-split on the device every step; the A scale then
-    covers max|Heff| + sum_d max|coef_d| max|ops_d|."""
+    The A operand is split once per generator (``split_operands``); each
+    instance takes its state scale from its own rho(0) on the device
+    (sqrt(n) ||rho(0)||_F bounds |rho_ij(t)|: the trace norm contracts) and
+    the kernel picks each B row's fixed-point quantum from the previous
+    stage's row bound, so nothing here waits for the GPU.  The final state
+    goes to ``rho_out`` (None: over ``rho``).  ``drive`` = (ops (n_drive, n,
+    n), coef (n_steps, n_drive)): Heff(t) = Heff - sum_d coef[k, d] ops[d],
+    re-split on the device every step; the A scale then covers max|Heff| +
+    sum_d max|coef_d| max|ops_d|."""
     lib = nat.require_device()
     why = split_supported(gen)
     if why is not None:
         raise ValueError('precision="split" does not support this generator: ' + why)
     B, n = rho.shape[0], gen.n
     mode, n_obs, Et, obs_stride = _split_obs(e_ops, n, gen.P, rho.device)
-    obs_out = torch.zeros((B, n_steps // obs_every, max(n_obs, 1)), dtype=CDT, device=rho.device)
+    obs_out = torch.empty((B, n_steps // obs_every, max(n_obs, 1)), dtype=CDT, device=rho.device)
     status = torch.zeros(1, dtype=torch.int32, device=rho.device)
-    m_diag = None
-    if gen.m is not None:
-        m_diag = torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous()
-    amax = float(gen.heff.abs().max().item())
     ws = None
     if drive is not None:
+        prep = None
+        m_diag = split_operands_mdiag(gen)
         dops, dcoef = drive
         if dcoef.shape[0] < n_steps:
             raise ValueError('drive coefficients cover %d steps, %d requested' % (dcoef.shape[0], n_steps))
-        amax += float((dcoef.abs().amax(0) * dops.abs().amax((-2, -1))).sum().item())
+        amax = heff_amax(gen) + float((dcoef.abs().amax(0) * dops.abs().amax((-2, -1))).sum().item())
         ws = torch.empty(int(lib.lime_lindblad_split_workspace(n, param_batch, dops.shape[0], n_steps)),
                          dtype=torch.uint8, device=rho.device)
-    rbound = float(torch.linalg.matrix_norm(rho).max().item()) * (n ** 0.5)
-    sb = _pow2_exponent(8192.0, rbound)
+        scale_a = _pow2_exponent(4096.0, amax)
+    else:
+        prep = split_operands(gen)
+        m_diag = prep['m_diag']
+        scale_a = prep['scale_a']
     d = nat.SplitDesc()
     d.n, d.batch, d.param_batch, d.n_steps = n, B, param_batch, n_steps
     d.obs_mode, d.n_obs, d.obs_every = mode, n_obs, obs_every
-    d.scale_a_log2 = _pow2_exponent(4096.0, amax)
-    d.scale_b_log2 = max(-60, min(60, sb))
+    d.scale_a_log2 = scale_a
+    d.scale_b_log2 = 0
+    d.auto_scale_b = 1
+    if prep is not None:
+        d.a_pieces, d.a_stride = prep['pieces'].data_ptr(), prep['stride']
+    if rho_out is not None:
+        d.rho_out = rho_out.data_ptr()
     d.ctas_per_sm = ctas_per_sm
     d.dt, d.trace_tol = float(dt), float(trace_tol)
     d.rho = rho.data_ptr()
@@ -318,6 +452,15 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
     if events is not None:
         events[1].record()
     return obs_out[:, :, :n_obs], None, status
+
+
+def split_operands_mdiag(gen: LindbladGenerator):
+    """The real diagonal of M (cached on the generator), or None."""
+    c = gen.split_cache
+    if 'm_diag' not in c:
+        c['m_diag'] = (None if gen.m is None else
+                       torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous())
+    return c['m_diag']
 
 
 def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
@@ -411,16 +554,33 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     return obs_out[:, :n_slots, :n_obs], None, status, work, redo
 
 
+def _host_hermitian(rho0):
+    """Hermiticity of a host rho0 (NumPy, scipy or CPU tensor), checked on
+    the host before the upload; None for a device tensor."""
+    a = _host_array(rho0)
+    if a is None:
+        return None
+    return bool(np.array_equal(a, np.conj(np.swapaxes(a, -1, -2))))
+
+
 def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
-            obs_every: int = 1, events=None, drive=None, defer: bool = False):
+            obs_every: int = 1, events=None, drive=None, defer: bool = False,
+            hermitian: bool | None = None):
     """Enqueue one propagation on the current stream; returns a closure that
     checks the status word (synchronising the stream) and assembles
     ``(obs, states, rho)``.  ``defer``: nothing after the launch waits for
-    the GPU (range retries of the streaming path happen in the closure)."""
+    the GPU (range retries of the streaming path happen in the closure).
+
+    Every kernel acts on Hermitian states; a non-Hermitian rho0 runs as its
+    two Hermitian parts.  Hermiticity is checked on the host for host
+    inputs; for a device tensor the batched split kernel checks it itself
+    (LIME_FLAG_NOT_HERMITIAN, after which the closure reruns the two parts),
+    the other paths compare rho0 with its adjoint on the device."""
     if obs_every < 1 or states_every < 0 or n_steps < 0:
         raise ValueError('obs_every must be >= 1, states_every >= 0, n_steps >= 0')
     device = gen.heff.device
+    herm = _host_hermitian(rho0) if hermitian is None else hermitian
     rho = as_device(rho0, device)
     if rho.dim() == 2:
         rho = rho.unsqueeze(0)
@@ -434,35 +594,47 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             B = gen.P
         else:
             raise ValueError('rho0 batch %d does not match %d generators' % (B, gen.P))
-    obs = prepare_obs(e_ops, n, gen.P, device) if precision == 'fp64' else None
-    herm = bool(torch.equal(rho, rho.mH))
-    if herm:
-        work = rho.clone().contiguous()
+    if precision not in ('fp64', 'split'):
+        raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
+    if precision == 'split' and states_every:
+        raise ValueError('precision="split" keeps the state on chip; states_every is not '
+                         'supported (use precision="fp64" for rholist output)')
+    batched_kernel = precision == 'split' and split_supported(gen) is None
+    optimistic = herm is None and batched_kernel
+    if herm is None and not batched_kernel:
+        herm = bool(torch.equal(rho, rho.mH))
+    out = None
+    if optimistic or herm:
+        if batched_kernel:
+            work = rho.contiguous()
+            out = torch.empty((B, n, n), dtype=CDT, device=device)
+        else:
+            work = rho.clone().contiguous()
     else:
         a, b = hermitian_parts(rho)
         work = torch.cat([a, b], 0).contiguous()
     redo = None
     if precision == 'fp64':
+        obs = prepare_obs(e_ops, n, gen.P, device)
         tol = 1e-9 if trace_tol is None else trace_tol
         o, s, status = _run_f64(gen, work, dt, n_steps, obs, obs_every, states_every, tol,
                                 param_batch=B, events=events, drive=drive)
-    elif precision == 'split':
-        if states_every:
-            raise ValueError('precision="split" keeps the state on chip; states_every is not '
-                             'supported (use precision="fp64" for rholist output)')
-        if split_supported(gen) is None:
-            tol = 1e-5 if trace_tol is None else trace_tol
-            o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
-                                      param_batch=B, events=events, drive=drive)
-        else:
-            o, s, status, work, redo = _run_stream(gen, work, dt, n_steps, e_ops, obs_every,
-                                                   param_batch=B, events=events, drive=drive,
-                                                   defer=defer)
+    elif batched_kernel:
+        tol = 1e-5 if trace_tol is None else trace_tol
+        o, s, status = _run_split(gen, work, dt, n_steps, e_ops, obs_every, tol,
+                                  param_batch=B, events=events, drive=drive, rho_out=out)
+        if out is not None:
+            work = out
     else:
-        raise ValueError("unknown precision %r (use 'fp64' or 'split')" % (precision,))
+        o, s, status, work, redo = _run_stream(gen, work, dt, n_steps, expand_e_ops(e_ops, n), obs_every,
+                                               param_batch=B, events=events, drive=drive,
+                                               defer=defer)
 
     def finish(check: bool = True):
         nonlocal o, status, work
+        if optimistic and int(status.item()) & nat.LIME_FLAG_NOT_HERMITIAN:
+            return _launch(gen, rho, dt, n_steps, e_ops, states_every, precision, trace_tol,
+                           obs_every, None, drive, defer, hermitian=False)(check)
         if redo is not None:
             for _ in range(3):
                 if not int(status.item()) & nat.LIME_FLAG_RANGE:
@@ -472,7 +644,7 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             flags = int(status.item())
             if flags:
                 raise nat.KernelFlagError(flags, 'lindblad RK4 (%s)' % precision)
-        if not herm:
+        if not (optimistic or herm):
             return (o[:B] + 1j * o[B:], None if s is None else s[:B] + 1j * s[B:],
                     work[:B] + 1j * work[B:])
         return o, s, work

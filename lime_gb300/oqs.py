@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from . import engine
-from .engine import DiagonalOps  # noqa: F401  (public: compact diagonal collapse operators)
+from .engine import DiagonalOps, Populations, SiteDephasing  # noqa: F401  (public: compact operator forms)
 from .result import Result
 
 
@@ -59,9 +59,13 @@ def _lindblad(H, rho0, c_ops, e_ops=None, Nt=1, dt=0.005, return_result=True,
     """
     if engine.is_ragged(H):
         return _lindblad_ragged(H, rho0, c_ops, e_ops, Nt, dt, precision, store_states, nout)
-    e_ops = [] if e_ops is None else list(e_ops)
+    if e_ops is None:
+        e_ops = []
+    elif not isinstance(e_ops, engine.Populations):
+        e_ops = list(e_ops)
     batched = _is_batched(H, rho0) or any(
-        isinstance(c, engine.DiagonalOps) and np.ndim(c.l) == 3 for c in (c_ops or []))
+        (isinstance(c, engine.DiagonalOps) and np.ndim(c.l) == 3) or
+        (isinstance(c, engine.SiteDephasing) and np.ndim(c.rates) == 2) for c in (c_ops or []))
     gen = engine.LindbladGenerator.build(H, c_ops)
     if return_result:
         obs, states, rho = engine.propagate(gen, rho0, dt, Nt, e_ops,
@@ -77,6 +81,7 @@ def _lindblad(H, rho0, c_ops, e_ops=None, Nt=1, dt=0.005, return_result=True,
             res.rholist = [_np(rho[0])] if not batched else _np(rho)
         return res
     obs, _, rho = engine.propagate(gen, rho0, dt, Nt, e_ops, precision=precision)
+    e_ops = engine.expand_e_ops(e_ops, gen.n)
     # observables before each step: Tr(E rho0), then after steps 0..Nt-2
     r0 = engine.as_device(rho0, rho.device)
     if r0.dim() == 2:

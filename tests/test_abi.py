@@ -109,6 +109,14 @@ def test_split_drive_workspace_query(lib):
     assert w(64, 1, 1, 10) % 256 == 0
 
 
+def test_split_prepared_bytes(lib):
+    b = lib.lime_lindblad_split_prepared_bytes
+    # three fp16 pieces of the 128 x 128 real block form per generator
+    assert b(64, 1) == 3 * 128 * 128 * 2 and b(8, 5) == 5 * b(8, 1)
+    assert b(0, 1) == 0 and b(65, 1) == 0 and b(8, 0) == 0
+    assert lib.lime_lindblad_split_prepare(None, None) == -1
+
+
 def _c_layout(struct_name, fields):
     prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "lime_gb300.h"', 'int main(void){',
             'printf("%zu\\n", sizeof({}));'.format(struct_name)]
@@ -121,6 +129,7 @@ def _c_layout(struct_name, fields):
     ('LimePrepareDesc', 'PrepareDesc'),
     ('LimeLindbladDesc', 'LindbladDesc'),
     ('LimeLindbladSplitDesc', 'SplitDesc'),
+    ('LimeLindbladSplitPrepareDesc', 'SplitPrepareDesc'),
     ('LimeAdjointDesc', 'AdjointDesc'),
     ('LimeRedfieldBuildDesc', 'RedfieldBuildDesc'),
     ('LimeRedfieldRK4Desc', 'RedfieldRK4Desc'),

@@ -108,3 +108,71 @@ def test_split_nonfinite_flag():
     with pytest.raises(_native.KernelFlagError) as ei:
         engine.propagate(gen, rho, 0.05, 5, precision='split')
     assert ei.value.flags & (_native.LIME_FLAG_NONFINITE | _native.LIME_FLAG_TRACE_DRIFT)
+
+
+def test_device_non_hermitian_start_reruns_as_two_parts():
+    """A device-tensor rho0 is checked by the kernel itself: a non-Hermitian
+    start raises LIME_FLAG_NOT_HERMITIAN and runs again as its two Hermitian
+    parts; the results match the FP64 path (which checks on the device)."""
+    from lime_gb300 import engine
+    m = chains.absorption_chain(20, chains.rng_for(4, child=5))
+    gen = engine.LindbladGenerator.build(m['H'], m['c_ops'])
+    rho = torch.as_tensor(m['mu'] @ chains.ground_dm(21), device='cuda')
+    o64, _, r64 = engine.propagate(gen, rho, 0.05, 300, [m['mu']])
+    osp, _, rsp = engine.propagate(gen, rho, 0.05, 300, [m['mu']], precision='split')
+    assert ((osp - o64).abs().max() / o64.abs().max()).item() < COR_TOL
+    assert (rsp - r64).abs().max().item() < POP_TOL
+
+
+def test_hermiticity_flag_and_untouched_input():
+    """One perturbed element makes one instance non-Hermitian: the kernel
+    flags it; a Hermitian device start is propagated into a new tensor and
+    the input is left as it was."""
+    from lime_gb300 import _native, engine
+    w, c_ops = _ensemble(12, 3, 20)
+    gen = engine.LindbladGenerator.build(w['H'], c_ops)
+    rho = torch.as_tensor(np.broadcast_to(w['rho0'], (3, 12, 12)).copy(), device='cuda')
+    keep = rho.clone()
+    o1, _, r1 = engine.propagate(gen, rho, 0.05, 20, chains.population_ops(12), precision='split')
+    assert torch.equal(rho, keep) and r1.data_ptr() != rho.data_ptr()
+    bad = rho.clone()
+    bad[1, 3, 5] += 1e-9
+    # the kernel's own verdict on the device tensor
+    _, _, st = engine._run_split(gen, bad, 0.05, 20, None, 1, 1e-5, param_batch=3,
+                                 rho_out=torch.empty_like(bad))
+    assert int(st.item()) & _native.LIME_FLAG_NOT_HERMITIAN
+    # the public call reruns the two Hermitian parts
+    _, _, r2 = engine.propagate(gen, bad, 0.05, 20, precision='split')
+    _, _, r64 = engine.propagate(gen, bad, 0.05, 20)
+    assert (r2 - r64).abs().max().item() < POP_TOL
+
+
+def test_prepared_operand_matches_in_kernel_split():
+    """The A operand prepared once per generator and the one split inside
+    the kernel are the same pieces: bitwise identical results."""
+    from lime_gb300 import _native, engine
+    lib = _native.require_device()
+    w, c_ops = _ensemble(40, 5, 50)
+    gen = engine.LindbladGenerator.build(w['H'], c_ops)
+    prep = engine.split_operands(gen)
+    rho = torch.as_tensor(np.broadcast_to(w['rho0'], (5, 40, 40)).copy(), device='cuda')
+    outs = []
+    for use in (True, False):
+        out = torch.empty_like(rho)
+        obs = torch.empty((5, 50, 40), dtype=torch.complex128, device='cuda')
+        st = torch.zeros(1, dtype=torch.int32, device='cuda')
+        d = _native.SplitDesc()
+        d.n, d.batch, d.param_batch, d.n_steps = 40, 5, 5, 50
+        d.obs_mode, d.n_obs, d.obs_every = 1, 40, 1
+        d.scale_a_log2, d.auto_scale_b = prep['scale_a'], 1
+        d.dt, d.trace_tol = 0.05, 1e-5
+        d.rho, d.rho_out = rho.data_ptr(), out.data_ptr()
+        d.heff, d.heff_stride = gen.heff.data_ptr(), 40 * 40
+        d.m_diag, d.m_stride = prep['m_diag'].data_ptr(), 40
+        d.obs_out, d.status = obs.data_ptr(), st.data_ptr()
+        if use:
+            d.a_pieces, d.a_stride = prep['pieces'].data_ptr(), prep['stride']
+        _native.check(lib.lime_lindblad_rk4_split(d, engine._stream_ptr()), 'split')
+        assert int(st.item()) == 0
+        outs.append((obs, out))
+    assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
