@@ -64,6 +64,9 @@ def parse():
                    help='run only the uneven-batch leg and print its JSON')
     p.add_argument('--adjoint-only', action='store_true',
                    help='run only the adjoint/forward leg and print its JSON')
+    p.add_argument('--errors-only', action='store_true',
+                   help='run only the full-horizon split-vs-FP64 error leg and print its JSON')
+    p.add_argument('--no-errors', action='store_true')
     p.add_argument('--adjoint-batch', type=int, default=256)
     p.add_argument('--ragged-batch', type=int, default=1024)
     p.add_argument('--ragged-sizes', default='8,16,32,64,128,256',
@@ -186,6 +189,10 @@ def gpu_arm(args, rank, world, local):
         if rank == 0:
             print(json.dumps(adjoint_leg(torch, dev, batch=args.adjoint_batch)))
         return
+    if args.errors_only:
+        if rank == 0:
+            print(json.dumps(full_horizon_leg(torch, dev)))
+        return
     if args.ragged_only:
         if rank == 0:
             print(json.dumps(ragged_leg(torch, dev, batch=args.ragged_batch,
@@ -276,6 +283,9 @@ def gpu_arm(args, rank, world, local):
     rows = None
     if not args.no_rows and single:
         rows = rows_leg(torch, dev)
+    errors = None
+    if not args.no_errors and single:
+        errors = full_horizon_leg(torch, dev)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -289,9 +299,10 @@ def gpu_arm(args, rank, world, local):
     flop_per_inst_step = 64 * N_SITES ** 3   # 2 complex N^3 GEMMs per RHS, 4 RHS
     achieved_tf = B * K * flop_per_inst_step / tk / 1e12
     if path == 'fp64':
-        roof = {'bound': 'fp64', 'achieved': achieved_tf, 'peak': 1.25, 'unit': 'TFLOP/s',
-                'frac': achieved_tf / 1.25, 'traffic': None,
-                'peak_source': 'nominal GB300 FP64 (no measured FP64 peak available)'}
+        pk64 = fp64_gemm_tflops(torch, dev)
+        roof = {'bound': 'fp64', 'achieved': achieved_tf, 'peak': pk64, 'unit': 'TFLOP/s',
+                'frac': achieved_tf / pk64, 'traffic': None,
+                'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run, of measured'}
     else:
         pk = peaks.get('bf16_tflops_sustained') or 1700.0
         # issued tensor work: per stage 5 fp16 products of the 128x64x128 real block
@@ -332,6 +343,7 @@ def gpu_arm(args, rank, world, local):
         'redfield': red,
         'uneven_batch': rag,
         'other_workloads': rows,
+        'full_horizon_errors': errors,
         'cpu_baseline': cpu,
     }
     if rank == 0:
@@ -357,22 +369,30 @@ def fp64_leg(gen, rho0, pop_ops, K, obs_every, obs_split, torch, engine, k64=4, 
                                    l_dense=None, k_dense=0, shared=False)
     o64, _, _ = engine.propagate(sub, rho0[:n_err], DT, K, pop_ops, obs_every=max(1, min(obs_every, K)))
     err = (obs_split[:n_err] - o64).abs().max().item()
+    # the FP64 kernel's roofline: the algorithmic 64 N^3 flop per instance-step
+    # against the measured FP64 peak (the kernel performs half of them: one
+    # GEMM per stage through the Hermitian shortcut)
+    pk64 = fp64_gemm_tflops(torch, rho0.device)
+    alg = rate * 64 * gen.n ** 3 / 1e12
     return {'value': rate, 'unit': 'instance-steps/s',
             'sample': 'full ensemble, %d RK4 steps' % k64,
+            'roofline': {'bound': 'fp64', 'achieved_algorithmic': alg, 'achieved_performed': alg / 2,
+                         'peak': pk64, 'frac_performed': alg / 2 / pk64, 'unit': 'TFLOP/s',
+                         'peak_source': 'cuBLAS DGEMM 4096^3 measured in this run, of measured'},
             'split_max_population_error': err,
             'error_sample': 'first %d realisations, all %d steps, every %d-th step recorded'
                             % (n_err, K, max(1, min(obs_every, K)))}
 
 
-def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=0.05):
-    """Adjoint/forward cost on the differentiated absorption workload shape:
+def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=4096, checkpoint=64, sample=64, dt=0.05):
+    """Adjoint/forward cost on the differentiated absorption workload:
     129-dim chains (|g> + 128 sites), 256 disorder samples, dipole
     correlation <mu(t) mu(0)>, gradients w.r.t. every site energy, the bond
-    couplings and the dephasing rates, checkpointed segments.  Times a sample
-    of ``steps`` RK4 steps (the workload runs 4096) of the FP64 path and of
-    the tensor-core path, and reports the tensor-core gradients' deviation
-    from the FP64 ones."""
-    import numpy as np
+    couplings and the dephasing rates, checkpoint every 64 steps.  The
+    tensor-core path runs the full 4096-step horizon; the FP64 path (about
+    85 ms a step at this size) a ``sample``-step window with the same
+    checkpoint interval, on which the tensor-core gradients are also compared
+    with the FP64 ones."""
     from lime_gb300 import chains
     from lime_gb300.adjoint import chain_observables
     w = chains.absorption_ensemble(n_sites=n_sites, batch=batch, n_steps=steps, dt=dt)
@@ -385,24 +405,19 @@ def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=
     rho0 = mu @ torch.as_tensor(w['rho_g'], device=dev)
     E = [mu]
 
-    def fwd(req, precision):
+    def fwd(req, precision, n):
         e = eps.clone().requires_grad_(req)
         b = bond.clone().requires_grad_(req)
         g = gamma.clone().requires_grad_(req)
-        return (e, b, g), chain_observables(H0, e, b, g, rho0, E, dt, steps, site0=1,
+        return (e, b, g), chain_observables(H0, e, b, g, rho0, E, dt, n, site0=1,
                                             checkpoint=checkpoint, precision=precision)
 
-    out = {'workload': 'absorption chain dim %d, %d samples, dipole correlation, grads w.r.t. '
-                       '%d site energies + %d bonds + %d dephasing rates, checkpoint %d'
-                       % (N, batch, n_sites, n_sites - 1, n_sites, checkpoint),
-           'sample_steps': steps}
-    grads = {}
-    for precision in ('fp64', 'split'):
-        fwd(False, precision)   # warm
+    def timed(precision, n):
+        fwd(False, precision, min(n, checkpoint))   # warm
         torch.cuda.synchronize()
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         ev[0].record()
-        params, obs = fwd(True, precision)
+        params, obs = fwd(True, precision, n)
         ev[1].record()
         loss = obs.real.sum()   # a linear functional of C(t), as a spectrum is
         loss.backward()
@@ -410,16 +425,21 @@ def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=64, checkpoint=32, dt=
         torch.cuda.synchronize()
         tf = ev[0].elapsed_time(ev[1]) / 1e3
         tb = ev[1].elapsed_time(ev[2]) / 1e3
-        grads[precision] = [p.grad for p in params]
-        out[precision] = {'forward_s': tf, 'adjoint_s': tb, 'adjoint_over_forward': tb / tf}
-    out['path'] = 'fp64'                       # the headline ratio below is the FP64 one
-    out['forward_s'] = out['fp64']['forward_s']
-    out['adjoint_s'] = out['fp64']['adjoint_s']
-    out['adjoint_over_forward'] = out['fp64']['adjoint_over_forward']
+        return [p.grad for p in params], {'steps': n, 'checkpoint': checkpoint, 'forward_s': tf,
+                                          'adjoint_s': tb, 'adjoint_over_forward': tb / tf}
+
+    out = {'workload': 'absorption chain dim %d, %d samples, dipole correlation over %d steps, grads '
+                       'w.r.t. %d site energies + %d bonds + %d dephasing rates, checkpoint every %d steps'
+                       % (N, batch, steps, n_sites, n_sites - 1, n_sites, checkpoint)}
+    g64, out['fp64'] = timed('fp64', sample)
+    gsp_s, out['split_sample'] = timed('split', sample)
+    _, out['split'] = timed('split', steps)
     out['split_grad_rel_error'] = max(
-        float((a - b).abs().max().item() / max(b.abs().max().item(), 1e-300))
-        for a, b in zip(grads['split'], grads['fp64']))
-    out['split_adjoint_speedup_vs_fp64'] = out['fp64']['adjoint_s'] / out['split']['adjoint_s']
+        float((a - b).abs().max().item() / max(b.abs().max().item(), 1e-300)) for a, b in zip(gsp_s, g64))
+    out['split_grad_error_sample'] = '%d-step window, same checkpoint interval' % sample
+    out['split_adjoint_speedup_vs_fp64'] = out['fp64']['adjoint_s'] / out['split_sample']['adjoint_s']
+    out['adjoint_over_forward'] = out['split']['adjoint_over_forward']
+    out['path'] = 'split, full horizon (FP64 on the sample window)'
     return out
 
 
@@ -633,6 +653,121 @@ def rows_leg(torch, dev):
         'nt': 200, 'ntau': 200, 'fp64_s': res['fp64'][1], 'split_s': res['split'][1],
         'split_rel_error': float(np.max(np.abs(csp - c64)) / np.max(np.abs(c64)))}
     return out
+
+
+def full_horizon_leg(torch, dev):
+    """Split-precision error against FP64 over every configured workload's
+    full horizon, on a sample of its instances (the timed legs run shorter
+    samples of steps):
+      ensemble     32 of the 4096 realisations x 4000 steps, populations every
+                   10 steps, vs the library's FP64 kernel
+      uneven       one chain of every N in {8..256} (two N = 8 chains packed
+                   into one instance), 3 dense collapse operators, 2000
+                   steps, 4 populations each, through the public uneven call
+      absorption   the dipole correlation of two 129-dimensional chains over
+                   4096 steps (relative to max |C|)
+      redfield     N = 96 (Liouville dimension 9216), two right-hand sides,
+                   all 96 populations every 10 steps, 2000 steps
+    The FP64 side of the last three is the PyTorch FP64 RK4 of
+    tests/fp64_torch.py (whole-GPU cuBLAS calls; the library's FP64 kernels
+    run one CTA per instance and would take minutes on these few large
+    instances), which the tests anchor to the library's FP64 kernels at
+    1e-12."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, 'tests'))
+    import fp64_torch
+    from lime_gb300 import chains, engine
+    from lime_gb300.engine import Populations, SiteDephasing
+    from lime_gb300.redfield import redfield_tensor, propagate_vec_split
+    out = {}
+
+    def clock(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    # ensemble (N = 64 dephasing chains)
+    w = chains.disorder_ensemble(n=N_SITES, batch=32, n_steps=FULL_STEPS)
+    gen = engine.LindbladGenerator.build(w['H'], [SiteDephasing(np.repeat(w['gamma'][:, None], N_SITES, 1))],
+                                         device=dev)
+    pops = Populations(N_SITES)
+    (osp, _, _), tsp = clock(lambda: engine.propagate(gen, w['rho0'], DT, FULL_STEPS, pops,
+                                                      precision='split', obs_every=10))
+    (o64, _, _), t64 = clock(lambda: engine.propagate(gen, w['rho0'], DT, FULL_STEPS, pops, obs_every=10))
+    out['ensemble_n64'] = {'sample': '32 realisations x %d steps, 64 populations every 10 steps' % FULL_STEPS,
+                           'max_population_error': (osp - o64).abs().max().item(),
+                           'reference': 'library FP64 kernel', 'split_s': tsp, 'fp64_s': t64}
+
+    # uneven batch
+    sizes = (8, 8, 16, 32, 64, 128, 256)
+    rng = np.random.default_rng(20261203 + 3)
+    H, C, R0, E = [], [], [], []
+    for n in sizes:
+        h, c = chains.uneven_chain(n, rng)
+        H.append(h)
+        C.append(c)
+        R0.append(chains.ground_dm(n))
+        E.append(chains.population_ops(n)[:4])
+    res, tsp = clock(lambda: engine.propagate_ragged(H, R0, DT, 2000, C, E, precision='split'))
+    errs, t64 = {}, 0.0
+    for i, n in enumerate(sizes):
+        g = engine.LindbladGenerator.build(H[i], C[i], device=dev)
+        (o, _), t = clock(lambda: fp64_torch.lindblad_rk4(g, torch.as_tensor(R0[i], device=dev)[None], DT, 2000,
+                                                          torch.as_tensor(np.stack(E[i]), device=dev),
+                                                          hermitian=True))
+        t64 += t
+        errs['N%d' % n] = max(errs.get('N%d' % n, 0.0), (res[0][i] - o[0]).abs().max().item())
+    out['uneven_batch'] = {'sample': 'chains N = %s, 3 dense collapse operators, 2000 steps, 4 populations each'
+                                     % ','.join(str(x) for x in sizes),
+                           'max_population_error': max(errs.values()), 'per_size': errs,
+                           'reference': 'PyTorch FP64 RK4', 'split_s': tsp, 'fp64_s': t64}
+
+    # absorption shape: dipole correlation, dimension 129
+    w = chains.absorption_ensemble(n_sites=128, batch=2, n_steps=4096)
+    gen = engine.LindbladGenerator.build(w['H'], [SiteDephasing(np.r_[0.0, np.full(128, w['gamma'])])],
+                                         device=dev)
+    mu = torch.as_tensor(w['mu'], device=dev)
+    rho = mu @ torch.as_tensor(w['rho_g'], device=dev)
+    (osp, _, _), tsp = clock(lambda: engine.propagate(gen, rho, w['dt'], 4096, [mu], precision='split'))
+    (o64, _), t64 = clock(lambda: fp64_torch.lindblad_rk4(gen, rho, w['dt'], 4096, mu[:, None]))
+    out['absorption_dim129'] = {'sample': 'dipole correlation <mu(t) mu(0)> of 2 chains x 4096 steps',
+                                'max_correlation_rel_error': ((osp - o64).abs().max() / o64.abs().max()).item(),
+                                'reference': 'PyTorch FP64 RK4', 'split_s': tsp, 'fp64_s': t64}
+
+    # dense Redfield superoperator
+    w = chains.redfield_chain(n=96, n_rhs=2, cfg=5)
+    R, evecs = redfield_tensor(w['H'], w['a_ops'], w['spectra'], device=dev)
+    V = torch.as_tensor(evecs, dtype=torch.complex128, device=dev)
+    r0 = V.mH @ torch.as_tensor(w['rho0'], dtype=torch.complex128, device=dev) @ V
+    Eeb = torch.stack([V.mH @ torch.as_tensor(e, dtype=torch.complex128, device=dev) @ V
+                       for e in chains.population_ops(96)])
+    (osp, _, rsp), tsp = clock(lambda: propagate_vec_split((R.R, 96), r0, 0.05, 2000, list(Eeb), obs_every=10))
+    (o64, r64), t64 = clock(lambda: fp64_torch.redfield_rk4(R.R, r0, 0.05, 2000, Eeb, obs_every=10))
+    out['redfield_dim9216'] = {'sample': '2 right-hand sides x 2000 steps, 96 populations every 10 steps',
+                               'max_population_error': (osp - o64).abs().max().item(),
+                               'max_state_error': (rsp - r64).abs().max().item(),
+                               'reference': 'PyTorch FP64 RK4', 'split_s': tsp, 'fp64_s': t64}
+    out['bar'] = 'populations <= 1e-6 absolute, correlations <= 1e-6 relative to max |C|'
+    return out
+
+
+def fp64_gemm_tflops(torch, dev, n=4096):
+    """Measured FP64 peak of this GPU: cuBLAS DGEMM n^3, best of three
+    (CUDA events); the denominator of the FP64 path's roofline."""
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    a @ a
+    best = None
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ a
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        best = t if best is None else min(best, t)
+    return 2.0 * n ** 3 / best / 1e12
 
 
 def e2e_leg(wl, K, path, dev):
