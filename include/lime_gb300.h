@@ -59,6 +59,9 @@ typedef enum {
 #define LIME_FLAG_NOT_HERMITIAN 0x10 /* rho(0) is not Hermitian: the batched */
                                    /* split kernel's results are invalid;   */
                                    /* run its two Hermitian parts instead   */
+#define LIME_FLAG_BOUNDS      0x20 /* bounds-checked build (LIME_CHECK)    */
+                                   /* only: an index left its buffer; the   */
+                                   /* access was skipped                    */
 
 /* ------------------------------------------------------------------ */
 /* Generator preparation                                               */
@@ -488,6 +491,12 @@ int lime_lindblad_split_prepare(const LimeLindbladSplitPrepareDesc* d, void* str
  *           general Lindblad paths with its operand copies withheld: the
  *           MMA and epilogue waits expire, the tile aborts      -> TIMEOUT
  *   kind 3  the same tile with its copies issued (control)       -> 0
+ *   kind 4  bounds-checked build (liblime_gb300_check.so) only: the
+ *           same tile told that its A operand holds one piece fewer than
+ *           it reads; the producer's extent check refuses that copy, so
+ *           nothing is read past the buffer, and the tile aborts
+ *                                          -> LIME_FLAG_BOUNDS | TIMEOUT
+ *           (the regular build returns LIME_ERR_UNSUPPORTED)
  * ws (kinds 2, 3; 16-byte aligned): lime_wait_selftest_workspace() bytes =
  * 10 zero operand pieces of 16 KB followed by 128 float row scales (1.0);
  * the control checks that the tile of zero operands comes out zero

@@ -10,7 +10,9 @@ import ctypes
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, 'liblime_gb300.so')
+# LIME_GB300_LIBRARY selects another build of the same ABI, e.g. the
+# bounds-checked liblime_gb300_check.so (lime_gb300.build.build(check=True))
+LIB_PATH = os.environ.get('LIME_GB300_LIBRARY') or os.path.join(HERE, 'liblime_gb300.so')
 
 c_int32 = ctypes.c_int32
 c_int64 = ctypes.c_int64
@@ -23,6 +25,7 @@ LIME_FLAG_TRACE_DRIFT = 0x2
 LIME_FLAG_TIMEOUT = 0x4
 LIME_FLAG_RANGE = 0x8
 LIME_FLAG_NOT_HERMITIAN = 0x10
+LIME_FLAG_BOUNDS = 0x20
 
 
 class LimeError(RuntimeError):
@@ -49,6 +52,8 @@ class KernelFlagError(RuntimeError):
             names.append('split-precision operand outside its fixed-point range')
         if flags & LIME_FLAG_NOT_HERMITIAN:
             names.append('rho(0) is not Hermitian')
+        if flags & LIME_FLAG_BOUNDS:
+            names.append('an index left its buffer (bounds-checked build)')
         super().__init__('%s: %s (flags 0x%x)' % (where, ', '.join(names) or 'unknown', flags))
 
 

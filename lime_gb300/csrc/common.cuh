@@ -29,6 +29,26 @@ __device__ __forceinline__ void cfma(double2& c, double2 a, double2 b) {
 }
 __device__ __forceinline__ bool cfinite(double2 a) { return isfinite(a.x) && isfinite(a.y); }
 
+// ---------------------------------------------------------------- bounds checks
+// The bounds-checked build (-DLIME_CHECK, liblime_gb300_check.so) checks the
+// byte range [off, off + len) of the accesses whose offsets come from tile,
+// piece and instance arithmetic against the extent of their buffer: a range
+// outside [0, extent) raises LIME_FLAG_BOUNDS in the kernel's status word and
+// the access is skipped (never a trap).  In the regular build the check is
+// compiled away.
+__device__ __forceinline__ bool in_bounds(size_t off, size_t len, size_t extent, int32_t* status) {
+#ifdef LIME_CHECK
+  if (off > extent || len > extent - off) {
+    if (status) atomicOr(status, LIME_FLAG_BOUNDS);
+    return false;
+  }
+#else
+  (void)off; (void)len; (void)extent; (void)status;
+#endif
+  return true;
+}
+constexpr size_t kNoExtent = ~(size_t)0;   // extent of a buffer the caller did not describe
+
 // ---------------------------------------------------------------- block reductions
 template <int NT>
 __device__ __forceinline__ double block_sum(double v, double* red) {

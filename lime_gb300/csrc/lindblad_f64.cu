@@ -108,6 +108,8 @@ struct RK4Args {
   int n_drive;
   const double2* drive_ops;
   const double* drive_coef;
+  // extents for the bounds-checked build (elements of obs_out and states)
+  size_t obs_elems = kNoExtent, states_elems = kNoExtent;
 };
 
 template <int TM>
@@ -214,8 +216,9 @@ __global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
       }
       sr = block_sum<kThreads>(sr, red);
       si = block_sum<kThreads>(si, red);
-      if (threadIdx.x == 0)
-        a.obs_out[((int64_t)b * a.obs_per_inst + oslot) * a.n_obs + o] = make_double2(sr, si);
+      const size_t oi = ((size_t)b * a.obs_per_inst + oslot) * a.n_obs + o;
+      if (threadIdx.x == 0 && in_bounds(oi * 16, 16, a.obs_elems * 16, a.status))
+        a.obs_out[oi] = make_double2(sr, si);
     }
     if (a.trace_tol > 0.0) {
       double t = 0.0;
@@ -226,7 +229,9 @@ __global__ void __launch_bounds__(kThreads) lindblad_rk4_f64_kernel(RK4Args a) {
     if (a.states && ((gstep + 1) % a.states_every) == 0) {
       const int slot = (gstep + 1) / a.states_every - 1;
       double2* dst = a.states + ((int64_t)b * a.states_per_inst + slot) * nn;
-      for (int64_t e = threadIdx.x; e < nn; e += kThreads) dst[e] = rho[e];
+      if (in_bounds((((size_t)b * a.states_per_inst + slot) * nn) * 16, (size_t)nn * 16, a.states_elems * 16,
+                    a.status))
+        for (int64_t e = threadIdx.x; e < nn; e += kThreads) dst[e] = rho[e];
     }
   }
   if (flags) atomicOr(a.status, flags);
@@ -545,6 +550,8 @@ extern "C" int lime_lindblad_rk4_f64(const LimeLindbladDesc* d, void* stream) {
   a.obs_every = d->obs_every > 0 ? d->obs_every : 1;
   a.obs_per_inst = d->n_steps / a.obs_every;
   a.states = reinterpret_cast<double2*>(d->states);
+  a.obs_elems = (size_t)d->batch * a.obs_per_inst * (d->n_obs > 0 ? d->n_obs : 0);
+  a.states_elems = (size_t)d->batch * a.states_per_inst * nn;
   a.ws = reinterpret_cast<double2*>(d->workspace);
   a.tr0 = reinterpret_cast<double*>(reinterpret_cast<char*>(d->workspace) +
                                     (size_t)d->batch * f64::ws_mats(d->k_dense) * nn * sizeof(double2));

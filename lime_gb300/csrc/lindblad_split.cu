@@ -128,6 +128,9 @@ struct Args {
   int auto_b;                                // per-instance B scale from ||rho(0)||_F
   int n_prefetch;                            // instances per CTA whose inputs are prefetched to L2
   double2* rho_out;                          // final state (may equal rho)
+  // extents for the bounds-checked build (elements of rho / rho_out and
+  // obs_out, uint4 words of a_pieces)
+  size_t rho_elems = kNoExtent, obs_elems = kNoExtent, a_words = kNoExtent;
 };
 
 __device__ __forceinline__ double block_sum(double v, double* red, int t) {
@@ -406,7 +409,11 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
 #pragma unroll
           for (int qq = 0; qq < 2; ++qq)
 #pragma unroll
-            for (int c4 = 0; c4 < 4; ++c4) v[piece][qq][c4] = src[a_piece_index(piece, qq, h, c4, r)];
+            for (int c4 = 0; c4 < 4; ++c4) {
+              const size_t w = (size_t)p * a.a_stride + a_piece_index(piece, qq, h, c4, r);
+              v[piece][qq][c4] = in_bounds(w * 16, 16, a.a_words * 16, a.status) ? src[a_piece_index(piece, qq, h, c4, r)]
+                                                                                   : make_uint4(0, 0, 0, 0);
+            }
 #pragma unroll
         for (int piece = 0; piece < 3; ++piece)
 #pragma unroll
@@ -447,7 +454,9 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       for (int e = t; e < kN * kN; e += kThreads) {
         const int ii = e >> 6, jj = e & 63;
         double2 z = make_double2(0.0, 0.0);
-        if (ii < n && jj < n) z = r0[ii * n + jj];
+        if (ii < n && jj < n &&
+            in_bounds(((size_t)b * n * n + ii * n + jj) * 16, 16, a.rho_elems * 16, a.status))
+          z = r0[ii * n + jj];
         stg[stage_index(ii, jj)] = z;
       }
     }
@@ -704,11 +713,13 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
       if (((gstep + 1) % a.obs_every) == 0) {
         const int slot = (gstep + 1) / a.obs_every - 1;
         double2* orow = a.obs_out + ((int64_t)b * a.obs_per_inst + slot) * a.n_obs;
+        const size_t obase = ((size_t)b * a.obs_per_inst + slot) * a.n_obs;
         const double dval =
             diag_owner ? fpconv::scale_pow2(fpconv::widen_f32(rho_d) + fpconv::widen_f32(S.rlo[i * 128 + r]), -S.eb)
                        : 0.0;
         if (a.obs_mode == 1) {
-          if (diag_owner && i < a.n_obs) orow[i] = make_double2(dval, 0.0);
+          if (diag_owner && i < a.n_obs && in_bounds((obase + i) * 16, 16, a.obs_elems * 16, a.status))
+            orow[i] = make_double2(dval, 0.0);
         } else if (a.obs_mode == 2) {
           const double2* E0 = a.obs_ops + p * a.obs_stride;
           for (int o = 0; o < a.n_obs; ++o) {
@@ -734,7 +745,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
             }
             const double sr = fpconv::scale_pow2(block_sum((double)pr, S.red[0], t), -S.eb);
             const double si = fpconv::scale_pow2(block_sum((double)pi, S.red[1], t), -S.eb);
-            if (t == 0) orow[o] = make_double2(sr, si);
+            if (t == 0 && in_bounds((obase + o) * 16, 16, a.obs_elems * 16, a.status)) orow[o] = make_double2(sr, si);
           }
         }
         if (a.trace_tol > 0.0) {
@@ -775,7 +786,7 @@ __global__ void __launch_bounds__(kThreads, 2) lindblad_rk4_split_kernel(Args a)
 #pragma unroll 4
       for (int e = t; e < n * n; e += kThreads) {
         const int ii = e / n, jj = e - ii * n;
-        out[e] = stg[stage_index(ii, jj)];
+        if (in_bounds(((size_t)b * n * n + e) * 16, 16, a.rho_elems * 16, a.status)) out[e] = stg[stage_index(ii, jj)];
       }
     }
     __syncthreads();   // smax / rlo of this instance are no longer read
@@ -970,6 +981,9 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   a.a_stride = d->a_stride / 16;
   a.auto_b = d->auto_scale_b != 0;
   a.rho_out = reinterpret_cast<double2*>(d->rho_out ? d->rho_out : d->rho);
+  a.rho_elems = (size_t)d->batch * d->n * d->n;
+  a.obs_elems = (size_t)d->batch * a.obs_per_inst * (d->n_obs > 0 ? d->n_obs : 0);
+  a.a_words = (size_t)(d->a_stride ? pb : 1) * split::kAPieceU4;
   cudaStream_t st = (cudaStream_t)stream;
   const bool driven = d->n_drive > 0;
   if (driven) {

@@ -58,6 +58,10 @@ struct Args {
   float* stage_store;                 // finish_kernel: also store the stage input here ([B][W][np]) or null
   int32_t* status;
   uint32_t max_wait;
+  // buffer extents for the bounds-checked build: bytes of one A1 / A2 piece
+  // set and of one B1 / B2 piece buffer, floats of one [B][W][np] state array
+  size_t a1_bytes = kNoExtent, a2_bytes = kNoExtent, b1_bytes = kNoExtent, b2_bytes = kNoExtent;
+  size_t st_floats = kNoExtent;
 };
 
 __device__ __forceinline__ size_t inst_floats(const Args& a) { return (size_t)a.W * a.np; }
@@ -129,6 +133,9 @@ __device__ __forceinline__ void assemble_f(const Args& a, int b, int jj, int y, 
 __device__ __forceinline__ void update8(const Args& a, int b, int jj, int y, const float (&f)[8], bool& bad,
                                         bool& range) {
   const size_t base = (size_t)b * inst_floats(a);
+  if (!in_bounds((base + (size_t)jj * a.np + y) * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float),
+                 a.status))
+    return;
   float sv[8];
   sg::rk4_stage8(a.rk, a.Phi + base, a.Plo + base, a.Acc + base, (size_t)jj * a.np + y, f, sv, bad);
   if (a.keep_s) sg::st8(a.Sn + base + (size_t)jj * a.np + y, sv);
@@ -139,7 +146,8 @@ __device__ __forceinline__ void update8(const Args& a, int b, int jj, int y, con
   }
   const bool im = jj >= a.np;
   const size_t boff = (size_t)b * a.NT * a.KC1 * kPiece;
-  sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, im ? jj - a.np : jj, im, sv);
+  sg::scatter_cplx8(a.B1n[0] + boff, a.B1n[1] + boff, a.KC1, a.np, a.np, y, im ? jj - a.np : jj, im, sv,
+                    a.b1_bytes - boff, a.status);
 }
 
 // kZ = false: GEMM 1 (X and Y_k rows); kZ = true: GEMM 2 and the stage update.
@@ -165,6 +173,9 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
   T.row_inv = (kZ ? a.rinv2 : a.rinv1) + ((size_t)g * MT + mt) * kBM;
   T.inv_sb = kZ ? a.inv_sy : (a.sb_exp_dev != nullptr ? ldexpf(1.f, -*a.sb_exp_dev) : a.inv_sb);
   T.max_wait = a.max_wait;
+  T.a_avail = (kZ ? a.a2_bytes : a.a1_bytes) - aoff;
+  T.b_avail = (kZ ? a.b2_bytes : a.b1_bytes) - boff;
+  T.status = a.status;
   const float* ft = S.tile();
   if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
     const int u = t - sg::kEpiFirst, ew = u >> 5;
@@ -178,10 +189,11 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
         const int jl = (wi >> 2) * 8 + nlo;
         const int dl = ((wi & 3) * 4 + glo) * 8;
         const int R = mt * kBM + dl;
-        if (R < np) {
+        const size_t xo = (size_t)b * inst_floats(a) + (size_t)(nt * kBN + jl) * np + R;
+        if (R < np && in_bounds(xo * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status)) {
           float v[8];
           sg::ld8(ft + jl * kFStride + dl, v);
-          sg::st8(a.Xg + (size_t)b * inst_floats(a) + (size_t)(nt * kBN + jl) * np + R, v);
+          sg::st8(a.Xg + xo, v);
         }
       }
       // ---- Y_k rows (blocks 1..K): Y^dag into B2, runs of 8 columns of one row
@@ -206,7 +218,8 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
             v[e] = __fmul_rn(im ? -y : y, a.sy);
             range |= !(fabsf(v[e]) <= sg::kBMax);
           }
-          sg::scatter_cplx8(B20, B21, a.KC2, a.K * np, np, (blk - 1) * np + x, yrow, im, v);
+          sg::scatter_cplx8(B20, B21, a.KC2, a.K * np, np, (blk - 1) * np + x, yrow, im, v,
+                            a.b2_bytes - (size_t)b * a.NT * a.KC2 * kPiece, a.status);
         }
       }
     } else {
@@ -769,6 +782,8 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   a.sb_exp_dev = nullptr;
   a.status = d->status;
   a.max_wait = 1u << 26;
+  a.a1_bytes = L.a1; a.a2_bytes = L.a2; a.b1_bytes = L.b1; a.b2_bytes = L.b2;
+  a.st_floats = L.st / sizeof(float);
   int64_t launches = 0;
 
   const int per_g = L.MT1 * 128 + (K > 0 ? L.MT2 * 128 : 0);
@@ -892,6 +907,8 @@ extern "C" int lime_lindblad_adjoint_stream(const LimeLindbladAdjointStreamDesc*
   af.Plo = reinterpret_cast<float*>(w); w += L.st;
   af.Acc = reinterpret_cast<float*>(w); w += L.st;
   w = reinterpret_cast<uint8_t*>(d->workspace) + L.total;   // past the forward layout (and its slack)
+  af.a1_bytes = L.a1; af.a2_bytes = L.a2; af.b1_bytes = L.b1; af.b2_bytes = L.b2;
+  af.st_floats = L.st / sizeof(float);
   lsm::Args aa = af;                                          // the adjoint generator: own A pieces
   for (int i = 0; i < 3; ++i) { aa.A1[i] = ca.A1[i] = w; w += L.a1; }
   aa.rinv1 = ca.rinv1 = reinterpret_cast<float*>(w); w += L.r1;

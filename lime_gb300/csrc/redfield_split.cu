@@ -42,6 +42,9 @@ struct StageArgs {
   double* obs;                       // observable pass: [R][n_obs] complex, accumulated
   int32_t* status;
   uint32_t max_wait;
+  // extents for the bounds-checked build: bytes of one A and one B piece
+  // buffer, floats of one state array
+  size_t a_bytes = kNoExtent, b_bytes = kNoExtent, st_floats = kNoExtent;
 };
 
 // kObserve = false: one RK4 stage, Y = L S over the full K, fused stage
@@ -71,6 +74,9 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
   T.row_inv = a.row_inv + (size_t)mt * kBM;
   T.inv_sb = a.inv_sb;
   T.max_wait = a.max_wait;
+  T.a_avail = a.a_bytes - (size_t)mt * a.KC * kPiece;
+  T.b_avail = a.b_bytes - (size_t)nt * a.KC * kPiece;
+  T.status = a.status;
   const float* ft = S.tile();
   if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
     const int u = t - sg::kEpiFirst, ew = u >> 5;
@@ -99,6 +105,9 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
         const int dl = ((wi & 3) * 4 + glo) * 8;
         const int jj = nt * kBN + jl, d = mt * kBM + dl;
         float f[8], sv[8];
+        if (!in_bounds(((size_t)jj * a.Dp + d) * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float),
+                       a.status))
+          continue;
         sg::ld8(ft + jl * kFStride + dl, f);
         sg::rk4_stage8(k4, a.Phi, a.Plo, a.Acc, (size_t)jj * a.Dp + d, f, sv, bad);
 #pragma unroll
@@ -107,7 +116,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
           range |= !(fabsf(sv[i]) <= sg::kBMax);
         }
         const bool im = jj >= a.Rp;
-        sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, im ? jj - a.Rp : jj, im, sv);
+        sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, im ? jj - a.Rp : jj, im, sv, a.b_bytes, a.status);
       }
       if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
       if (range) atomicOr(a.status, LIME_FLAG_RANGE);
@@ -155,7 +164,7 @@ __global__ void init_state_kernel(StageArgs a, const double2* rho, int D, int R)
     const size_t e = (size_t)jj * a.Dp + d;
     sg::st8(a.Phi + e, hv);
     sg::st8(a.Plo + e, lv);
-    sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, j, im, x);
+    sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, j, im, x, a.b_bytes, a.status);
   }
   if (range) atomicOr(a.status, LIME_FLAG_RANGE);
 }
@@ -263,6 +272,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   a.Phi = Phi; a.Plo = Plo; a.Acc = Acc;
   a.status = d->status;
   a.max_wait = 1u << 26;
+  a.a_bytes = L.apiece; a.b_bytes = L.bpiece; a.st_floats = (size_t)W * Dp;
   // first B input = rho0
   a.Bn[0] = B[0]; a.Bn[1] = B[1];
   const size_t tot = (size_t)W * Dp;
@@ -284,6 +294,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   if (MTo > 0) {
     ao.MT = MTo;
     ao.A[0] = Ep[0]; ao.A[1] = Ep[1]; ao.A[2] = Ep[2];
+    ao.a_bytes = L.epiece;
     ao.row_inv = row_inv + (size_t)MT * 128;
     ao.n_obs = d->n_obs;
     const int groups = KC / sg::kGroup;

@@ -5,7 +5,9 @@
 // returns, so the context stays usable.  These kernels make such waits run
 // out on purpose — on a barrier that nothing completes, or in the streaming
 // GEMM tile with its operand copies withheld — next to controls in which
-// the waits complete.
+// the waits complete.  Kind 4 (bounds-checked build only) refuses an
+// operand copy whose declared extent is too short and reports
+// LIME_FLAG_BOUNDS.
 
 #include "stream_gemm.cuh"
 
@@ -28,8 +30,12 @@ __global__ void mbar_kernel(int arrive, uint32_t max_wait, int32_t* status) {
 
 // One 128 x 128 tile of zero operands over two K chunks; the parked result
 // must be zero.
+// short_extent (bounds-checked build): the tile is told its A operand holds
+// one piece fewer than the two chunks it reads, so the producer's extent
+// check refuses the second copy (no access leaves the buffer) and the tile
+// aborts.
 __global__ void __launch_bounds__(sg::kThreads, 1)
-    tile_kernel(const uint8_t* ws, int withhold, uint32_t max_wait, int32_t* status) {
+    tile_kernel(const uint8_t* ws, int withhold, int short_extent, uint32_t max_wait, int32_t* status) {
   extern __shared__ uint8_t smem_raw[];
   sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   sg::setup(S);
@@ -42,6 +48,9 @@ __global__ void __launch_bounds__(sg::kThreads, 1)
   T.inv_sb = 1.f;
   T.max_wait = max_wait;
   T.withhold = withhold;
+  T.a_avail = short_extent ? (size_t)(kTileChunks - 1) * sg::kPiece : (size_t)kTileChunks * sg::kPiece;
+  T.b_avail = (size_t)kTileChunks * sg::kPiece;
+  T.status = status;
   if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
     const int u = threadIdx.x - sg::kEpiFirst;
     const float* ft = S.tile();
@@ -61,7 +70,10 @@ using namespace lime;
 extern "C" size_t lime_wait_selftest_workspace(void) { return selftest::kTileBytes; }
 
 extern "C" int lime_wait_selftest(int kind, uint32_t max_wait, const void* ws, int32_t* status, void* stream) {
-  if (kind < 0 || kind > 3 || !status || max_wait == 0) return LIME_ERR_ARG;
+  if (kind < 0 || kind > 4 || !status || max_wait == 0) return LIME_ERR_ARG;
+#ifndef LIME_CHECK
+  if (kind == 4) return LIME_ERR_UNSUPPORTED;   // the extent check exists only in the bounds-checked build
+#endif
   if (kind >= 2 && (!ws || (reinterpret_cast<uintptr_t>(ws) & 15) != 0)) return LIME_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (kind < 2) {
@@ -70,7 +82,7 @@ extern "C" int lime_wait_selftest(int kind, uint32_t max_wait, const void* ws, i
     LIME_CUDA_TRY(cudaFuncSetAttribute(selftest::tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sg::kSmemBytes));
     selftest::tile_kernel<<<1, sg::kThreads, sg::kSmemBytes, st>>>(static_cast<const uint8_t*>(ws), kind == 2,
-                                                                    max_wait, status);
+                                                                    kind == 4, max_wait, status);
   }
   LIME_CUDA_TRY(cudaGetLastError());
   count_launch();

@@ -100,9 +100,10 @@ __device__ __forceinline__ void split_b(float x, float& v0, float& v1) {
 }
 
 // 8 scaled B values at (row n, k..k+7), k % 8 == 0, as two 16-byte stores
-// per piece; `neg` stores their negatives.
+// per piece; `neg` stores their negatives.  avail: bytes of each piece
+// buffer from B0 / B1 (checked in the bounds-checked build).
 __device__ __forceinline__ void store_b8(uint8_t* B0, uint8_t* B1, int KC, int n, int k, const float (&x)[8],
-                                         bool neg) {
+                                         bool neg, size_t avail = kNoExtent, int32_t* status = nullptr) {
   uint32_t h0[4], h1[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
@@ -116,6 +117,7 @@ __device__ __forceinline__ void store_b8(uint8_t* B0, uint8_t* B1, int KC, int n
   }
   const uint32_t sg = neg ? 0x80008000u : 0u;
   const size_t off = piece_off(KC, n, k);
+  if (!in_bounds(off, 16, avail, status)) return;
   *reinterpret_cast<uint4*>(B0 + off) = make_uint4(h0[0] ^ sg, h0[1] ^ sg, h0[2] ^ sg, h0[3] ^ sg);
   *reinterpret_cast<uint4*>(B1 + off) = make_uint4(h1[0] ^ sg, h1[1] ^ sg, h1[2] ^ sg, h1[3] ^ sg);
 }
@@ -126,13 +128,14 @@ __device__ __forceinline__ void store_b8(uint8_t* B0, uint8_t* B1, int KC, int n
 // imaginary parts, scaled.  Kp, Np: padded K and N (row/column offsets of
 // the second block).
 __device__ __forceinline__ void scatter_cplx8(uint8_t* B0, uint8_t* B1, int KC, int Kp, int Np, int k, int j,
-                                              bool im, const float (&x)[8]) {
+                                              bool im, const float (&x)[8], size_t avail = kNoExtent,
+                                              int32_t* status = nullptr) {
   if (!im) {
-    store_b8(B0, B1, KC, j, k, x, false);             // Sr at (k, j)
-    store_b8(B0, B1, KC, j + Np, Kp + k, x, false);   // Sr at (K + k, N + j)
+    store_b8(B0, B1, KC, j, k, x, false, avail, status);             // Sr at (k, j)
+    store_b8(B0, B1, KC, j + Np, Kp + k, x, false, avail, status);   // Sr at (K + k, N + j)
   } else {
-    store_b8(B0, B1, KC, j, Kp + k, x, true);         // -Si at (K + k, j)
-    store_b8(B0, B1, KC, j + Np, k, x, false);        // Si at (k, N + j)
+    store_b8(B0, B1, KC, j, Kp + k, x, true, avail, status);         // -Si at (K + k, j)
+    store_b8(B0, B1, KC, j + Np, k, x, false, avail, status);        // Si at (k, N + j)
   }
 }
 
@@ -200,6 +203,10 @@ struct Tile {
   float inv_sb;            // inverse B scale
   uint32_t max_wait;       // bound on every mbarrier poll loop
   int withhold = 0;        // self-test only: the producer issues no copies, so every wait expires
+  // bytes readable from A[i] / B[i] (checked in the bounds-checked build:
+  // a chunk past them is not copied, and the tile aborts)
+  size_t a_avail = kNoExtent, b_avail = kNoExtent;
+  int32_t* status = nullptr;
 };
 
 // TMEM allocation and barrier set-up; every thread of the CTA calls it.
@@ -257,6 +264,11 @@ __device__ __forceinline__ bool mainloop(Smem& S, const Tile& T) {
         const uint32_t ph = (uint32_t)(c / kStages) & 1u;
         if (!tc::mbar_wait_bounded(&S.empty[s], ph ^ 1u, T.max_wait)) { atomicExch(&S.abort, 1); break; }
         if (*(volatile int*)&S.abort || T.withhold) break;
+        if (!in_bounds((size_t)(T.c0 + c) * kPiece, kPiece, T.a_avail, T.status) ||
+            !in_bounds((size_t)(T.c0 + c) * kPiece, kPiece, T.b_avail, T.status)) {
+          atomicExch(&S.abort, 1);
+          break;
+        }
         issued = c + 1;
         tc::mbar_arrive_expect_tx(&S.full[s], 5 * kPiece);
         const size_t off = (size_t)(T.c0 + c) * kPiece;

@@ -50,6 +50,8 @@ def test_bad_arguments_rejected(lib):
     assert lib.lime_wait_selftest(0, 0, None, status.data_ptr(), stream) < 0
     assert lib.lime_wait_selftest(2, 100, None, status.data_ptr(), stream) < 0
     assert lib.lime_wait_selftest(0, 100, None, None, stream) < 0
+    # kind 4 (the extent check) exists only in the bounds-checked build
+    assert lib.lime_wait_selftest(4, 100, None, status.data_ptr(), stream) == -2
 
 
 def test_context_usable_after_expired_waits(lib):
