@@ -230,6 +230,75 @@ typedef struct {
 size_t lime_redfield_rk4_f64_workspace(int32_t n, int32_t n_rhs);
 int lime_redfield_rk4_f64(const LimeRedfieldRK4Desc* d, void* stream);
 
+/* The assembly step of lime_redfield_build_f64 alone, from caller-supplied
+ * factors (for a differentiable generator whose factors the caller builds
+ * and differentiates; replaces the same loop of redfield_tensor,
+ * lime/oqs.py:528-579):
+ *   evals [n]; a_eig, lam [k][n][n] complex128 with Lam_k = C_k o A_k;
+ *   p, q [n][n] complex128: P = sum_k A_k Lam_k, Q = sum_k Lam_k^dag A_k;
+ *   R [n^2][n^2] complex128 out (the closed form above). */
+typedef struct {
+  int32_t n, k;
+  const double* evals;
+  const double* a_eig;
+  const double* lam;
+  const double* p;
+  const double* q;
+  double* R;
+} LimeRedfieldAssembleDesc;
+
+int lime_redfield_assemble_f64(const LimeRedfieldAssembleDesc* d, void* stream);
+
+/* Adjoint of lime_redfield_assemble_f64 (no counterpart in the reference,
+ * which has no gradients): given G = dl/dconj(R) (the gradient of a real
+ * loss l in the convention dl = Re sum conj(G) dR), writes the gradients of
+ * the factors in the same convention: grad_evals [n] (real), grad_a and
+ * grad_lam [k][n][n], grad_p and grad_q [n][n] (all complex128, overwritten).
+ * The chain rule through Lam_k = C_k o A_k, P, Q, A_k = V^dag a_k V and
+ * eigh(H) is the caller's (O(N^3 K) against the O(N^4 K) done here). */
+typedef struct {
+  int32_t n, k;
+  const double* a_eig;
+  const double* lam;
+  const double* G;
+  double* grad_evals;
+  double* grad_a;
+  double* grad_lam;
+  double* grad_p;
+  double* grad_q;
+} LimeRedfieldAssembleAdjointDesc;
+
+int lime_redfield_assemble_adjoint_f64(const LimeRedfieldAssembleAdjointDesc* d, void* stream);
+
+/* Discrete adjoint of lime_redfield_rk4_f64 over one checkpoint segment of
+ * seg_steps steps starting at step0 (no counterpart in the reference): the
+ * segment is recomputed from ckpt storing every stage input y_i, then per
+ * step from the last: lam += Et^dag g for the observables recorded after the
+ * step (obs_grad [n_slots][n_rhs][n_obs] = dl/dconj(obs), laid out like
+ * lime_redfield_rk4_f64's obs_out), the adjoint RK4 stages with L^dag
+ * (a_4 = dt/6 lam, a_3 = dt/3 lam + dt L^dag a_4, a_2 = dt/3 lam +
+ * dt/2 L^dag a_3, a_1 = dt/6 lam + dt/2 L^dag a_2, lam += sum_i L^dag a_i),
+ * grad_R += sum_i a_i y_i^dag and grad_obs[o][j][i] += g_o conj(rho[i][j]).
+ *   ckpt    [n^2][n_rhs] state at step0 (column r = vec rho_r)
+ *   lam     [n^2][n_rhs] in: adjoint state after the segment; out: at step0
+ *   grad_R  [n^2][n^2] accumulated; grad_obs [n_obs][n][n] accumulated or NULL
+ *   workspace lime_redfield_adjoint_f64_workspace(n, n_rhs, seg_steps) bytes */
+typedef struct {
+  int32_t n, n_rhs, seg_steps, step0, n_obs, obs_every, n_slots;
+  double dt;
+  const double* R;
+  const double* ckpt;
+  double* lam;
+  const double* obs_ops;
+  const double* obs_grad;
+  double* grad_R;
+  double* grad_obs;
+  void* workspace;        size_t workspace_bytes;
+} LimeRedfieldAdjointDesc;
+
+size_t lime_redfield_adjoint_f64_workspace(int32_t n, int32_t n_rhs, int32_t seg_steps);
+int lime_redfield_adjoint_f64(const LimeRedfieldAdjointDesc* d, void* stream);
+
 /* The same RK4 on the tcgen05 tensor cores in split precision: per stage
  * one GEMM [Yr|Yi] = [Lr|Li] . [[Sr,Si],[-Si,Sr]] with the operands streamed
  * by bulk copies from pre-tiled fp16 pieces (A = R, each row scaled by a

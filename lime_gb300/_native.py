@@ -134,6 +134,29 @@ class RedfieldBuildDesc(ctypes.Structure):
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
 
 
+class RedfieldAssembleDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('k', c_int32),
+                ('evals', c_void_p), ('a_eig', c_void_p), ('lam', c_void_p),
+                ('p', c_void_p), ('q', c_void_p), ('R', c_void_p)]
+
+
+class RedfieldAssembleAdjointDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('k', c_int32),
+                ('a_eig', c_void_p), ('lam', c_void_p), ('G', c_void_p),
+                ('grad_evals', c_void_p), ('grad_a', c_void_p), ('grad_lam', c_void_p),
+                ('grad_p', c_void_p), ('grad_q', c_void_p)]
+
+
+class RedfieldAdjointDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('seg_steps', c_int32), ('step0', c_int32),
+                ('n_obs', c_int32), ('obs_every', c_int32), ('n_slots', c_int32),
+                ('dt', c_double),
+                ('R', c_void_p), ('ckpt', c_void_p), ('lam', c_void_p),
+                ('obs_ops', c_void_p), ('obs_grad', c_void_p),
+                ('grad_R', c_void_p), ('grad_obs', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
+
+
 class RedfieldRK4Desc(ctypes.Structure):
     _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('n_steps', c_int32), ('n_obs', c_int32),
                 ('obs_every', c_int32), ('states_every', c_int32),
@@ -198,6 +221,10 @@ SIGNATURES = [
     ('lime_lindblad_adjoint_f64', c_int32, [ctypes.POINTER(AdjointDesc), c_void_p]),
     ('lime_redfield_build_f64_workspace', c_size_t, [c_int32, c_int32]),
     ('lime_redfield_build_f64', c_int32, [ctypes.POINTER(RedfieldBuildDesc), c_void_p]),
+    ('lime_redfield_assemble_f64', c_int32, [ctypes.POINTER(RedfieldAssembleDesc), c_void_p]),
+    ('lime_redfield_assemble_adjoint_f64', c_int32, [ctypes.POINTER(RedfieldAssembleAdjointDesc), c_void_p]),
+    ('lime_redfield_adjoint_f64_workspace', c_size_t, [c_int32, c_int32, c_int32]),
+    ('lime_redfield_adjoint_f64', c_int32, [ctypes.POINTER(RedfieldAdjointDesc), c_void_p]),
     ('lime_redfield_rk4_f64_workspace', c_size_t, [c_int32, c_int32]),
     ('lime_redfield_rk4_f64', c_int32, [ctypes.POINTER(RedfieldRK4Desc), c_void_p]),
     ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32, c_int32]),

@@ -14,61 +14,10 @@
 // stage combination fused into the GEMM epilogue.  FP64 throughout; this is
 // the exact path (DFMA-bound on GB300).
 
-#include "common.cuh"
+#include "gemm_f64.cuh"
 
 namespace lime {
 namespace rf {
-
-constexpr int kThreads = 256;
-constexpr int kTile = 64;   // CTA output tile (64 x 64), 4 x 4 complex per thread
-constexpr int kKC = 16;
-
-// Tiled complex GEMM over one output tile; loaders give A(i,k) and B(k,j)
-// (zero outside), epi(i, j, value) consumes the result.
-template <class LA, class LB, class EPI>
-__device__ void gemm_tile(int M, int N, int K, int i0, int j0, LA la, LB lb, EPI epi) {
-  __shared__ double2 As[kTile][kKC + 1];
-  __shared__ double2 Bs[kKC][kTile + 1];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  double2 acc[4][4];
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) acc[u][v] = cz();
-  for (int k0 = 0; k0 < K; k0 += kKC) {
-    for (int idx = threadIdx.x; idx < kTile * kKC; idx += kThreads) {
-      const int r = idx / kKC, c = idx % kKC;
-      const int gi = i0 + r, gk = k0 + c;
-      As[r][c] = (gi < M && gk < K) ? la(gi, gk) : cz();
-    }
-    for (int idx = threadIdx.x; idx < kTile * kKC; idx += kThreads) {
-      const int r = idx / kTile, c = idx % kTile;
-      const int gk = k0 + r, gj = j0 + c;
-      Bs[r][c] = (gk < K && gj < N) ? lb(gk, gj) : cz();
-    }
-    __syncthreads();
-#pragma unroll 4
-    for (int kk = 0; kk < kKC; ++kk) {
-      double2 a[4], b[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) a[u] = As[ty + 16 * u][kk];
-#pragma unroll
-      for (int v = 0; v < 4; ++v) b[v] = Bs[kk][tx + 16 * v];
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 4; ++v) cfma(acc[u][v], a[u], b[v]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int u = 0; u < 4; ++u)
-#pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const int gi = i0 + ty + 16 * u, gj = j0 + tx + 16 * v;
-      if (gi < M && gj < N) epi(gi, gj, acc[u][v]);
-    }
-}
 
 // ---------------------------------------------------------------- assembly
 __global__ void lam_kernel(int n, int k, const double2* A, const double* C, int64_t c_stride, double2* Lam) {
@@ -130,41 +79,6 @@ __global__ void __launch_bounds__(kThreads) assemble_kernel(BuildArgs a) {
   gemm_tile(D, D, 2 * K, blockIdx.y * kTile, blockIdx.x * kTile, la, lb, epi);
 }
 
-// ---------------------------------------------------------------- RK4 stages
-struct StageArgs {
-  int D, R, stage;
-  double dt;
-  const double2* L;     // D x D
-  const double2* S;     // stage input, D x R
-  double2* P;           // state, D x R
-  double2* acc;         // D x R
-  double2* Snext;       // next stage input, D x R
-};
-
-__global__ void __launch_bounds__(kThreads) stage_kernel(StageArgs a) {
-  const int D = a.D, R = a.R;
-  auto la = [&](int i, int k) -> double2 { return a.L[(int64_t)i * D + k]; };
-  auto lb = [&](int k, int j) -> double2 { return a.S[(int64_t)k * R + j]; };
-  const double dt = a.dt, dt2 = a.dt / 2.0;
-  const int s = a.stage;
-  auto epi = [&](int i, int j, double2 f) {
-    const int64_t e = (int64_t)i * R + j;
-    if (s == 0) {
-      a.acc[e] = f;
-      a.Snext[e] = cadd(a.P[e], cscale(f, dt2));
-    } else if (s < 3) {
-      a.acc[e] = cadd(a.acc[e], cscale(f, 2.0));
-      a.Snext[e] = cadd(a.P[e], cscale(f, s == 2 ? dt : dt2));
-    } else {
-      const double2 sum = cadd(a.acc[e], f);
-      const double2 nr = cadd(a.P[e], cscale(make_double2(sum.x / 6., sum.y / 6.), dt));
-      a.P[e] = nr;
-      a.Snext[e] = nr;
-    }
-  };
-  gemm_tile(D, R, D, blockIdx.y * kTile, blockIdx.x * kTile, la, lb, epi);
-}
-
 // obs[r][o] = sum_ij E_o[j][i] rho_r[i][j]  (D-dot per observable and RHS)
 __global__ void observe_kernel(int n, int R, int n_obs, const double2* Eops, const double2* P, double2* out) {
   const int64_t D = (int64_t)n * n;
@@ -215,6 +129,21 @@ extern "C" int lime_redfield_build_f64(const LimeRedfieldBuildDesc* d, void* str
   rf::assemble_kernel<<<grid, rf::kThreads, 0, st>>>(a);
   LIME_CUDA_TRY(cudaGetLastError());
   count_launch(3);
+  return LIME_OK;
+}
+
+extern "C" int lime_redfield_assemble_f64(const LimeRedfieldAssembleDesc* d, void* stream) {
+  if (!d || d->n <= 0 || d->k <= 0) return LIME_ERR_ARG;
+  if (!d->evals || !d->a_eig || !d->lam || !d->p || !d->q || !d->R) return LIME_ERR_ARG;
+  if ((int64_t)d->n * d->n > 46340) return LIME_ERR_UNSUPPORTED;
+  const int D = d->n * d->n;
+  rf::BuildArgs a{d->n, d->k, d->evals, reinterpret_cast<const double2*>(d->a_eig),
+                  reinterpret_cast<const double2*>(d->lam), reinterpret_cast<const double2*>(d->p),
+                  reinterpret_cast<const double2*>(d->q), reinterpret_cast<double2*>(d->R)};
+  dim3 grid((D + rf::kTile - 1) / rf::kTile, (D + rf::kTile - 1) / rf::kTile);
+  rf::assemble_kernel<<<grid, rf::kThreads, 0, (cudaStream_t)stream>>>(a);
+  LIME_CUDA_TRY(cudaGetLastError());
+  count_launch();
   return LIME_OK;
 }
 

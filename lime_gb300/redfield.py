@@ -134,7 +134,10 @@ def propagate_vec(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=None, 
     dev = Rd.device
     B = rho0_eb.shape[0]
     D = n * n
-    P = rho0_eb.reshape(B, D).transpose(0, 1).contiguous()          # D x B, column = vec rho
+    # D x B, column = vec rho; always a fresh buffer (the kernel writes it
+    # in place, and the input may itself be a view of an earlier result)
+    P = torch.empty((D, B), dtype=CDT, device=dev)
+    P.copy_(rho0_eb.reshape(B, D).transpose(0, 1))
     E = None
     n_obs = 0
     if e_eb is not None and len(e_eb):

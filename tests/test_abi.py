@@ -58,6 +58,9 @@ def test_null_descriptor_rejected(lib):
     assert lib.lime_redfield_rk4_split(None, None) == -1
     assert lib.lime_redfield_rk4_f64(None, None) == -1
     assert lib.lime_lindblad_adjoint_f64(None, None) == -1
+    assert lib.lime_redfield_assemble_f64(None, None) == -1
+    assert lib.lime_redfield_assemble_adjoint_f64(None, None) == -1
+    assert lib.lime_redfield_adjoint_f64(None, None) == -1
 
 
 def test_stream_descriptor_validation(lib):
@@ -133,6 +136,9 @@ def _c_layout(struct_name, fields):
     ('LimeAdjointDesc', 'AdjointDesc'),
     ('LimeRedfieldBuildDesc', 'RedfieldBuildDesc'),
     ('LimeRedfieldRK4Desc', 'RedfieldRK4Desc'),
+    ('LimeRedfieldAssembleDesc', 'RedfieldAssembleDesc'),
+    ('LimeRedfieldAssembleAdjointDesc', 'RedfieldAssembleAdjointDesc'),
+    ('LimeRedfieldAdjointDesc', 'RedfieldAdjointDesc'),
     ('LimeRedfieldSplitDesc', 'RedfieldSplitDesc'),
     ('LimeLindbladStreamDesc', 'LindbladStreamDesc'),
     ('LimeLindbladAdjointStreamDesc', 'AdjointStreamDesc'),
