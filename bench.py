@@ -67,6 +67,9 @@ def parse():
     p.add_argument('--errors-only', action='store_true',
                    help='run only the full-horizon split-vs-FP64 error leg and print its JSON')
     p.add_argument('--no-errors', action='store_true')
+    p.add_argument('--redfield-adjoint-only', action='store_true',
+                   help='run only the Redfield adjoint/forward leg and print its JSON')
+    p.add_argument('--no-redfield-adjoint', action='store_true')
     p.add_argument('--adjoint-batch', type=int, default=256)
     p.add_argument('--ragged-batch', type=int, default=1024)
     p.add_argument('--ragged-sizes', default='8,16,32,64,128,256',
@@ -193,6 +196,10 @@ def gpu_arm(args, rank, world, local):
         if rank == 0:
             print(json.dumps(full_horizon_leg(torch, dev)))
         return
+    if args.redfield_adjoint_only:
+        if rank == 0:
+            print(json.dumps(redfield_adjoint_leg(torch, dev)))
+        return
     if args.ragged_only:
         if rank == 0:
             print(json.dumps(ragged_leg(torch, dev, batch=args.ragged_batch,
@@ -286,6 +293,9 @@ def gpu_arm(args, rank, world, local):
     errors = None
     if not args.no_errors and single:
         errors = full_horizon_leg(torch, dev)
+    radj = None
+    if not args.no_redfield_adjoint and single:
+        radj = redfield_adjoint_leg(torch, dev)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool
@@ -344,6 +354,7 @@ def gpu_arm(args, rank, world, local):
         'uneven_batch': rag,
         'other_workloads': rows,
         'full_horizon_errors': errors,
+        'redfield_adjoint': radj,
         'cpu_baseline': cpu,
     }
     if rank == 0:
@@ -441,6 +452,69 @@ def adjoint_leg(torch, dev, n_sites=128, batch=256, steps=4096, checkpoint=64, s
     out['adjoint_over_forward'] = out['split']['adjoint_over_forward']
     out['path'] = 'split, full horizon (FP64 on the sample window)'
     return out
+
+
+def redfield_adjoint_leg(torch, dev, n=96, n_rhs=512, steps=128, checkpoint=64, dt=0.05):
+    """Adjoint/forward cost of the differentiable Redfield workload at the
+    dense superoperator's size (N = 96, Liouville dimension 9216, 512
+    right-hand sides): gradients of all 96 populations' weighted sum with
+    respect to the 96 site energies, the coupling J, 96 bath coupling
+    strengths and the Ohmic reorganisation energy, on the tensor cores
+    (split forward and backward), checkpoint every 64 steps, over a
+    ``steps``-step sample of the 2000-step workload (the cost per step does
+    not depend on the horizon)."""
+    import numpy as np
+    from lime_gb300 import chains
+    from lime_gb300.redfield_grad import redfield_observables, ohmic_spectrum
+    w = chains.redfield_chain(n=n, n_rhs=n_rhs, cfg=5)
+    eps0 = torch.tensor(np.real(np.diag(w['H'])).copy(), device=dev)
+    off = torch.diag(torch.ones(n - 1, dtype=torch.float64, device=dev), 1)
+    proj = torch.eye(n, dtype=torch.float64, device=dev)
+    rho0 = torch.as_tensor(w['rho0'], device=dev)
+    E = torch.as_tensor(np.stack(chains.population_ops(n)), device=dev)
+    wts = torch.tensor(np.random.default_rng(5).normal(size=(n_rhs, steps, n)), device=dev)
+
+    def run(grad):
+        eps = eps0.clone().requires_grad_(grad)
+        J = torch.tensor(-0.1, dtype=torch.float64, device=dev, requires_grad=grad)
+        s = torch.ones(n, dtype=torch.float64, device=dev, requires_grad=grad)
+        lam = torch.tensor(0.05, dtype=torch.float64, device=dev, requires_grad=grad)
+        H = torch.diag(eps) + J * (off + off.T)
+        a_ops = s[:, None, None] * torch.diag_embed(proj)
+        obs = redfield_observables(H, a_ops, ohmic_spectrum(lam, 0.1, 0.025), rho0, E, dt, steps,
+                                   checkpoint=checkpoint, precision='split')
+        return (obs.real * wts).sum(), (eps, J, s, lam)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        out = fn()
+        b.record()
+        torch.cuda.synchronize()
+        return out, a.elapsed_time(b) / 1e3
+
+    with torch.no_grad():
+        run(False)                      # warm
+        _, tf = timed(lambda: run(False))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    ev[0].record()
+    loss, params = run(True)
+    ev[1].record()
+    loss.backward()
+    ev[2].record()
+    torch.cuda.synchronize()
+    tfg = ev[0].elapsed_time(ev[1]) / 1e3
+    tb = ev[1].elapsed_time(ev[2]) / 1e3
+    return {'workload': 'Redfield N=%d (Liouville dim %d), %d right-hand sides, weighted populations; grads '
+                        'w.r.t. %d site energies, J, %d bath coupling strengths and the reorganisation energy; '
+                        'checkpoint every %d steps; %d-step sample of the 2000-step workload'
+                        % (n, n * n, n_rhs, n, n, checkpoint, steps),
+            'path': 'split forward and backward (lime_redfield_rk4_split, lime_redfield_adjoint_split)',
+            'forward_s': tf, 'forward_with_checkpoints_s': tfg, 'adjoint_s': tb,
+            'adjoint_over_forward': tb / tf,
+            'grad_norms': [float(p.grad.abs().max().item()) for p in params]}
 
 
 def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k64=3):

@@ -334,6 +334,40 @@ typedef struct {
 size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs, int32_t n_obs);
 int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* stream);
 
+/* The discrete adjoint of lime_redfield_rk4_split over one checkpoint
+ * segment, on the tensor cores (no counterpart in the reference): the
+ * recursion of lime_redfield_adjoint_f64 with every generator application
+ * a streaming split-precision GEMM — the segment recomputed from ckpt with
+ * L, the adjoint stages with L^dag (a_i scaled per step by the power of two
+ * that maps (dt/2) max |lam| to 2^13 / 1.25 / 2^margin_log2), and the
+ * generator gradient sum_i a_i y_i^dag of each step as one GEMM of K = four
+ * stages x right-hand sides into an fp32 two-sum accumulator, added to
+ * grad_R at the end of the call.
+ *   ckpt, lam   [n_rhs][n^2] complex128 (row-major vec per right-hand side,
+ *               as lime_redfield_rk4_split's rho); lam in/out
+ *   scale_b_log2  the state scale of lime_redfield_rk4_split
+ *   obs_ops, obs_grad, grad_R, grad_obs as in lime_redfield_adjoint_f64
+ *   status    device int32: LIME_FLAG_RANGE (repeat with a larger margin)
+ *   workspace lime_redfield_adjoint_split_workspace(n, n_rhs, seg_steps,
+ *             n_obs) bytes, 1024-byte aligned */
+typedef struct {
+  int32_t n, n_rhs, seg_steps, step0, n_obs, obs_every, n_slots;
+  int32_t scale_b_log2, margin_log2;
+  double dt;
+  const double* R;
+  const double* ckpt;
+  double* lam;
+  const double* obs_ops;
+  const double* obs_grad;
+  double* grad_R;
+  double* grad_obs;
+  void* workspace;        size_t workspace_bytes;
+  int32_t* status;
+} LimeRedfieldAdjointSplitDesc;
+
+size_t lime_redfield_adjoint_split_workspace(int32_t n, int32_t n_rhs, int32_t seg_steps, int32_t n_obs);
+int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* General Lindblad RK4 on the tensor cores (split precision)           */
 /* ------------------------------------------------------------------ */

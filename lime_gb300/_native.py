@@ -157,6 +157,18 @@ class RedfieldAdjointDesc(ctypes.Structure):
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
 
 
+class RedfieldAdjointSplitDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('seg_steps', c_int32), ('step0', c_int32),
+                ('n_obs', c_int32), ('obs_every', c_int32), ('n_slots', c_int32),
+                ('scale_b_log2', c_int32), ('margin_log2', c_int32),
+                ('dt', c_double),
+                ('R', c_void_p), ('ckpt', c_void_p), ('lam', c_void_p),
+                ('obs_ops', c_void_p), ('obs_grad', c_void_p),
+                ('grad_R', c_void_p), ('grad_obs', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t),
+                ('status', c_void_p)]
+
+
 class RedfieldRK4Desc(ctypes.Structure):
     _fields_ = [('n', c_int32), ('n_rhs', c_int32), ('n_steps', c_int32), ('n_obs', c_int32),
                 ('obs_every', c_int32), ('states_every', c_int32),
@@ -225,6 +237,8 @@ SIGNATURES = [
     ('lime_redfield_assemble_adjoint_f64', c_int32, [ctypes.POINTER(RedfieldAssembleAdjointDesc), c_void_p]),
     ('lime_redfield_adjoint_f64_workspace', c_size_t, [c_int32, c_int32, c_int32]),
     ('lime_redfield_adjoint_f64', c_int32, [ctypes.POINTER(RedfieldAdjointDesc), c_void_p]),
+    ('lime_redfield_adjoint_split_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
+    ('lime_redfield_adjoint_split', c_int32, [ctypes.POINTER(RedfieldAdjointSplitDesc), c_void_p]),
     ('lime_redfield_rk4_f64_workspace', c_size_t, [c_int32, c_int32]),
     ('lime_redfield_rk4_f64', c_int32, [ctypes.POINTER(RedfieldRK4Desc), c_void_p]),
     ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32, c_int32]),

@@ -45,13 +45,35 @@ struct StageArgs {
   // extents for the bounds-checked build: bytes of one A and one B piece
   // buffer, floats of one state array
   size_t a_bytes = kNoExtent, b_bytes = kNoExtent, st_floats = kNoExtent;
+  // mode 0 (recompute): fp32 copy of the next stage input ([W][Dp]) or null
+  float* ystore = nullptr;
+  // mode 2 (adjoint stage i): adjoint state (fp32 pair), the step's sum of
+  // L^dag a_i, the next adjoint stage input a_{i-1} = c_l lam + c_y L^dag a_i
+  // ([W][Dp] each) and the device exponent of the adjoint B scale
+  float* Lhi = nullptr;
+  float* Llo = nullptr;
+  float* LAcc = nullptr;
+  float* anext = nullptr;
+  int adj_i = 0;
+  float c_l = 0.f, c_y = 0.f;
+  const int* sl_exp = nullptr;
+  // mode 3 (generator gradient): fp32 two-sum accumulator [2Dp][Dp] and the
+  // per-column inverse scales of the B operand ([Dp], shared by a column's
+  // real and imaginary block)
+  float* Ghi = nullptr;
+  float* Glo = nullptr;
+  const float* col_inv = nullptr;
 };
 
-// kObserve = false: one RK4 stage, Y = L S over the full K, fused stage
-// update.  kObserve = true: observables <E_o> = sum_d Et[o][d] P[d][r] of
-// the state held in Bc, K split over KS CTAs.
-template <bool kObserve>
+// kMode 0: one RK4 stage, Y = L S over the full K, fused stage update.
+// kMode 1: observables <E_o> = sum_d Et[o][d] P[d][r] of the state held in
+// Bc, K split over KS CTAs.  kMode 2: one stage of the discrete adjoint,
+// yb = L^dag a (A = the L^dag pieces, B = a), fused adjoint combination.
+// kMode 3: the generator gradient sum_i a_i y_i^dag of one step (A = the
+// adjoint stage inputs, B = the stage inputs), added to the accumulator.
+template <int kMode>
 __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
+  constexpr bool kObserve = kMode == 1;
   extern __shared__ uint8_t smem_raw[];
   sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int t = threadIdx.x, lane = t & 31;
@@ -72,7 +94,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
   T.c0 = c0;
   T.n_chunks = KC;
   T.row_inv = a.row_inv + (size_t)mt * kBM;
-  T.inv_sb = a.inv_sb;
+  T.inv_sb = (kMode == 2) ? ldexpf(1.f, -*a.sl_exp) : a.inv_sb;
   T.max_wait = a.max_wait;
   T.a_avail = a.a_bytes - (size_t)mt * a.KC * kPiece;
   T.b_avail = a.b_bytes - (size_t)nt * a.KC * kPiece;
@@ -94,6 +116,77 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
                       (double)ft[(sg::kEpiCols * hh + c) * kFStride + r]);
         }
       }
+    } else if (kMode == 2) {
+      // ---- adjoint stage: yb = L^dag a_i in runs of 8 rows; a_{i-1} or the new lam
+      const int nlo = lane & 7, glo = lane >> 3;
+      const float sl = ldexpf(1.f, *a.sl_exp);
+      bool range = false;
+#pragma unroll 1
+      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
+        const int jl = (wi >> 2) * 8 + nlo;
+        const int dl = ((wi & 3) * 4 + glo) * 8;
+        const int jj = nt * kBN + jl, d = mt * kBM + dl;
+        const size_t e = (size_t)jj * a.Dp + d;
+        if (!in_bounds(e * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status)) continue;
+        float f[8], l[8], acc[8];
+        sg::ld8(ft + jl * kFStride + dl, f);
+        sg::ld8(a.Lhi + e, l);
+        if (a.adj_i == 4) {
+          sg::st8(a.LAcc + e, f);
+        } else {
+          sg::ld8(a.LAcc + e, acc);
+          if (a.adj_i > 1) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] = __fadd_rn(acc[i], f[i]);
+            sg::st8(a.LAcc + e, acc);
+          } else {
+            float lo[8];
+            sg::ld8(a.Llo + e, lo);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) l[i] = rk4_final_f32(l[i], acc[i], f[i], 1.f, 0.f, lo[i]);
+            sg::st8(a.Lhi + e, l);
+            sg::st8(a.Llo + e, lo);
+          }
+        }
+        if (a.adj_i > 1) {
+          float nx[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) nx[i] = __fmaf_rn(a.c_l, l[i], __fmul_rn(a.c_y, f[i]));
+          sg::st8(a.anext + e, nx);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            nx[i] = __fmul_rn(nx[i], sl);
+            range |= !(fabsf(nx[i]) <= sg::kBMax);
+          }
+          const bool im = jj >= a.Rp;
+          sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, im ? jj - a.Rp : jj, im, nx, a.b_bytes,
+                            a.status);
+        }
+      }
+      if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+    } else if (kMode == 3) {
+      // ---- generator gradient: add the tile to the fp32 two-sum accumulator
+      // [column][row] (columns: Re G then Im G), runs of 8 rows
+      const int nlo = lane & 7, glo = lane >> 3;
+#pragma unroll 1
+      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
+        const int jl = (wi >> 2) * 8 + nlo;
+        const int dl = ((wi & 3) * 4 + glo) * 8;
+        const int jj = nt * kBN + jl;
+        const size_t e = (size_t)jj * a.Dp + mt * kBM + dl;
+        if (!in_bounds(e * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status)) continue;
+        float f[8], hi[8], lo[8];
+        sg::ld8(ft + jl * kFStride + dl, f);
+        const float cs = a.col_inv[jj < a.Dp ? jj : jj - a.Dp];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) f[i] = __fmul_rn(f[i], cs);
+        sg::ld8(a.Ghi + e, hi);
+        sg::ld8(a.Glo + e, lo);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) hi[i] = rk4_final_f32(hi[i], 0.f, f[i], 1.f, 0.f, lo[i]);
+        sg::st8(a.Ghi + e, hi);
+        sg::st8(a.Glo + e, lo);
+      }
     } else {
       // ---- fused RK4 stage update in runs of 8 rows: lane -> (column & 7, row run & 3)
       const int nlo = lane & 7, glo = lane >> 3;
@@ -110,6 +203,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
           continue;
         sg::ld8(ft + jl * kFStride + dl, f);
         sg::rk4_stage8(k4, a.Phi, a.Plo, a.Acc, (size_t)jj * a.Dp + d, f, sv, bad);
+        if (a.ystore != nullptr) sg::st8(a.ystore + (size_t)jj * a.Dp + d, sv);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           sv[i] = __fmul_rn(sv[i], a.sb);
@@ -125,14 +219,16 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
   sg::teardown(S, a.status);
 }
 
-// A pieces of generator rows (transposed = 0: element (row, kk) = L[row][kk])
-// or of observables (transposed = 1: element (o, a n + b) = E_o[b][a], so
-// that <E_o> = sum_d M[o][d] vec(rho)[d]).
+// A pieces of generator rows (transposed = 0: element (row, kk) = L[row][kk]),
+// of observables (transposed = 1: element (o, a n + b) = E_o[b][a], so
+// that <E_o> = sum_d M[o][d] vec(rho)[d]) or of the adjoint generator
+// (transposed = 2: element (row, kk) = conj(L[kk][row])).
 __global__ void convert_rows_kernel(const double2* M, int transposed, int n, int rows, int D, int Dp, int KC,
                                     uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
   const int row = blockIdx.x;
   auto elem = [&](int kk) -> double2 {
-    if (!transposed) return M[(size_t)row * D + kk];
+    if (transposed == 0) return M[(size_t)row * D + kk];
+    if (transposed == 2) return cconj(M[(size_t)kk * D + row]);
     const int ia = kk / n, ib = kk - ia * n;
     return M[(size_t)row * D + (size_t)ib * n + ia];
   };
@@ -164,9 +260,250 @@ __global__ void init_state_kernel(StageArgs a, const double2* rho, int D, int R)
     const size_t e = (size_t)jj * a.Dp + d;
     sg::st8(a.Phi + e, hv);
     sg::st8(a.Plo + e, lv);
+    if (a.ystore != nullptr) sg::st8(a.ystore + e, hv);
     sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, j, im, x, a.b_bytes, a.status);
   }
   if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// ---------------------------------------------------------------- discrete adjoint
+// (lime_redfield_adjoint_split; the recursion of lime_redfield_adjoint_f64)
+
+// EtF[o][a n + b] = E_o[b][a] as float pairs (re, im)
+__global__ void adj_et_kernel(const double2* E, int n_obs, int n, float2* EtF) {
+  const int D = n * n;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_obs * D; e += gridDim.x * blockDim.x) {
+    const int o = e / D, d = e % D, ia = d / n, ib = d % n;
+    const double2 v = E[(size_t)o * D + (size_t)ib * n + ia];
+    EtF[e] = make_float2((float)v.x, (float)v.y);
+  }
+}
+
+// lam = hi + lo (fp32 pair, planar [W][Dp]) from or into complex128 [R][D]
+__global__ void adj_lam_in_kernel(const double2* lam, int D, int R, int Dp, int Rp, float* Lhi, float* Llo) {
+  const size_t total = (size_t)R * D;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / D), d = (int)(e % D);
+    const double2 v = lam[e];
+    const size_t er = (size_t)r * Dp + d, ei = (size_t)(Rp + r) * Dp + d;
+    const float hr = (float)v.x, hi = (float)v.y;
+    Lhi[er] = hr;
+    Llo[er] = (float)(v.x - (double)hr);
+    Lhi[ei] = hi;
+    Llo[ei] = (float)(v.y - (double)hi);
+  }
+}
+__global__ void adj_lam_out_kernel(const float* Lhi, const float* Llo, int D, int R, int Dp, int Rp, double2* lam) {
+  const size_t total = (size_t)R * D;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / D), d = (int)(e % D);
+    const size_t er = (size_t)r * Dp + d, ei = (size_t)(Rp + r) * Dp + d;
+    lam[e] = make_double2((double)Lhi[er] + (double)Llo[er], (double)Lhi[ei] + (double)Llo[ei]);
+  }
+}
+
+// lam += Et^dag g (the observables recorded after the step, g [R][n_obs]
+// complex128, or none) and max |lam| of the step; one thread per (column
+// r, run of 8 rows d), both components
+__global__ void adj_src_kernel(float* Lhi, float* Llo, int D, int R, int Dp, int Rp, const float2* EtF, int n_obs,
+                               const double2* g, unsigned* lmax) {
+  const size_t runs = (size_t)Dp / 8, total = (size_t)Rp * runs;
+  float mx = 0.f;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(q / runs), d0 = (int)(q % runs) * 8;
+    const size_t er = (size_t)r * Dp + d0, ei = (size_t)(Rp + r) * Dp + d0;
+    float hr[8], hi[8];
+    sg::ld8(Lhi + er, hr);
+    sg::ld8(Lhi + ei, hi);
+    if (g != nullptr && r < R) {
+      float sr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, si[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      for (int o = 0; o < n_obs; ++o) {
+        const double2 gv = g[(size_t)r * n_obs + o];
+        const float gr = (float)gv.x, gi = (float)gv.y;
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          if (d0 + i < D) {
+            // conj(Et) g = (er gr + ei gi) + i (er gi - ei gr)
+            const float2 et = EtF[(size_t)o * D + d0 + i];
+            sr[i] = __fmaf_rn(et.x, gr, __fmaf_rn(et.y, gi, sr[i]));
+            si[i] = __fmaf_rn(et.x, gi, __fmaf_rn(-et.y, gr, si[i]));
+          }
+        }
+      }
+      float lr[8], li[8];
+      sg::ld8(Llo + er, lr);
+      sg::ld8(Llo + ei, li);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        hr[i] = rk4_final_f32(hr[i], 0.f, sr[i], 1.f, 0.f, lr[i]);
+        hi[i] = rk4_final_f32(hi[i], 0.f, si[i], 1.f, 0.f, li[i]);
+      }
+      sg::st8(Lhi + er, hr);
+      sg::st8(Llo + er, lr);
+      sg::st8(Lhi + ei, hi);
+      sg::st8(Llo + ei, li);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) mx = fmaxf(mx, fmaxf(fabsf(hr[i]), fabsf(hi[i])));
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(lmax, __float_as_uint(mx));
+}
+
+// exponent of the step's adjoint B scale: |a_i| <= bound max |lam| maps to
+// 2^13 / 1.25 / 2^margin; clears the maximum for the next step
+__global__ void adj_scale_kernel(unsigned* lmax, int* sl, float bound, int margin) {
+  const float m = __uint_as_float(*lmax) * bound;
+  int e = 0;
+  if (m > 0.f && isfinite(m)) {
+    e = (int)floorf(log2f(6553.6f / m)) - margin;
+    e = e < -60 ? -60 : (e > 60 ? 60 : e);
+  }
+  *sl = e;
+  *lmax = 0u;
+}
+
+// a_4 = dt/6 lam: fp32 copy and the scaled B pieces of the first adjoint stage
+__global__ void adj_start_kernel(StageArgs a, float dt6) {
+  const size_t runs = (size_t)a.Dp / 8, total = (size_t)a.W * runs;
+  const float sl = ldexpf(1.f, *a.sl_exp);
+  bool range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int jj = (int)(q / runs), d = (int)(q % runs) * 8;
+    const size_t e = (size_t)jj * a.Dp + d;
+    float x[8];
+    sg::ld8(a.Lhi + e, x);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) x[i] = __fmul_rn(dt6, x[i]);
+    sg::st8(a.anext + e, x);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      x[i] = __fmul_rn(x[i], sl);
+      range |= !(fabsf(x[i]) <= sg::kBMax);
+    }
+    const bool im = jj >= a.Rp;
+    sg::scatter_cplx8(a.Bn[0], a.Bn[1], a.KC, a.Dp, a.Rp, d, im ? jj - a.Rp : jj, im, x, a.b_bytes, a.status);
+  }
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// grad_E[o][b][a] += sum_r g[r][o] conj(rho[(a, b)][r]) for the observables
+// recorded after the step (rho planar [W][Dp] fp32); one thread per (o, d)
+__global__ void adj_grad_obs_kernel(const float* rho, const double2* g, int n_obs, int n, int R, int Dp, int Rp,
+                                    double2* gE) {
+  const int D = n * n;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_obs * D; e += gridDim.x * blockDim.x) {
+    const int o = e / D, d = e % D;
+    float vr = 0.f, vi = 0.f;
+    for (int r = 0; r < R; ++r) {
+      const double2 gv = g[(size_t)r * n_obs + o];
+      const float pr = rho[(size_t)r * Dp + d], pi = rho[(size_t)(Rp + r) * Dp + d];
+      // g conj(rho) = (gr pr + gi pi) + i (gi pr - gr pi)
+      vr = __fmaf_rn((float)gv.x, pr, __fmaf_rn((float)gv.y, pi, vr));
+      vi = __fmaf_rn((float)gv.y, pr, __fmaf_rn(-(float)gv.x, pi, vi));
+    }
+    const int ia = d / n, ib = d % n;
+    double2& t = gE[(size_t)o * D + (size_t)ib * n + ia];
+    t = make_double2(t.x + (double)vr, t.y + (double)vi);
+  }
+}
+
+// A pieces of the gradient GEMM: row d, K index kk = i Rp + r over the four
+// adjoint stage inputs (real parts in [0, 4Rp), imaginary in [4Rp, 8Rp)),
+// each row scaled by the power of two that brings its largest component
+// into [2^12, 2^13) and split as 64 k + two fp16 residuals (fp32
+// arithmetic: the inputs are fp32).  One CTA per row.
+__global__ void adj_g_convert_a_kernel(const float* astack, size_t st_floats, int Dp, int Rp, int KCg, uint8_t* A0,
+                                       uint8_t* A1, uint8_t* A2, float* row_inv) {
+  __shared__ float red[32];
+  const int row = blockIdx.x;
+  const int cols = 4 * Rp;
+  auto comp = [&](int k) -> float {   // k in [0, 8Rp)
+    const int c = k < cols ? 0 : 1, kk = k < cols ? k : k - cols;
+    const int i = kk / Rp, r = kk - i * Rp;
+    return astack[(size_t)i * st_floats + (size_t)(c * Rp + r) * Dp + row];
+  };
+  float mx = 0.f;
+  for (int k = threadIdx.x; k < 2 * cols; k += blockDim.x) mx = fmaxf(mx, fabsf(comp(k)));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    red[0] = m;
+  }
+  __syncthreads();
+  mx = red[0];
+  const bool live = mx > 0.f && isfinite(mx);
+  const int sh = live ? 12 - ilogbf(mx) : 0;
+  if (threadIdx.x == 0) row_inv[row] = live ? ldexpf(1.f, -sh) : 0.f;
+  for (int k = threadIdx.x; k < 2 * cols; k += blockDim.x) {
+    const float x = live ? ldexpf(comp(k), sh) : 0.f;   // |x| < 2^13
+    const float v0 = fminf(fmaxf(rintf(x * (1.f / 64.f)), -127.f), 127.f) * 64.f;
+    const float r1 = __fsub_rn(x, v0);                     // exact
+    const __half h1 = __float2half_rn(r1);
+    const __half h2 = __float2half_rn(__fsub_rn(r1, __half2float(h1)));
+    const size_t off = sg::piece_off(KCg, row, k);
+    *reinterpret_cast<__half*>(A0 + off) = __float2half_rn(v0);
+    *reinterpret_cast<__half*>(A1 + off) = h1;
+    *reinterpret_cast<__half*>(A2 + off) = h2;
+  }
+}
+
+// B pieces of the gradient GEMM from the step's stage inputs y_1..y_4
+// (ystep: four planar [W][Dp] arrays): B^T row c = [Re y(c, K) | Im y(c, K)],
+// row Dp + c = [-Im y | Re y] with K = i Rp + r: the [[Sr, Si], [-Si, Sr]]
+// form of S = conj(y), so that the GEMM gives [Re G | Im G] = A . y^dag.
+// Each column c (both of its B^T rows) is scaled by its own power of two,
+// bringing its largest component into [2^12, 2^13), so that small state
+// elements keep the fixed-point grid's relative precision; col_inv[c] gets
+// the inverse scale.  One CTA per column.
+__global__ void adj_g_convert_b_kernel(const float* ystep, size_t st_floats, int Dp, int Rp, int KCg, uint8_t* B0,
+                                       uint8_t* B1, float* col_inv) {
+  __shared__ float red[32];
+  const int c = blockIdx.x;
+  const int kruns = 4 * Rp / 8;
+  auto val = [&](int im, int k) -> float {   // component im of y at K index k
+    const int i = k / Rp, r = k - i * Rp;
+    return ystep[(size_t)i * st_floats + (size_t)(im * Rp + r) * Dp + c];
+  };
+  float mx = 0.f;
+  for (int k = threadIdx.x; k < 8 * Rp; k += blockDim.x) mx = fmaxf(mx, fabsf(val(k >= 4 * Rp, k % (4 * Rp))));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float m = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmaxf(m, red[w]);
+    red[0] = m;
+  }
+  __syncthreads();
+  mx = red[0];
+  const bool live = mx > 0.f && isfinite(mx);
+  const int sh = live ? 12 - ilogbf(mx) : 0;
+  if (threadIdx.x == 0) col_inv[c] = live ? ldexpf(1.f, -sh) : 0.f;
+  for (int q = threadIdx.x; q < 2 * kruns; q += blockDim.x) {
+    const int run = q % kruns, im = q / kruns, k0 = run * 8;
+    float x[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const float v = live ? ldexpf(val(im, k0 + e), sh) : 0.f;
+      x[e] = im ? -v : v;   // conj(y)
+    }
+    sg::scatter_cplx8(B0, B1, KCg, 4 * Rp, Dp, k0, c, im != 0, x);
+  }
+}
+
+// grad_R[row][col] += G accumulated ([2Dp][Dp]: Re G columns, then Im G)
+__global__ void adj_g_final_kernel(const float* Ghi, const float* Glo, int D, int Dp, double2* gR) {
+  const size_t total = (size_t)D * D;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const int col = (int)(e / D), row = (int)(e % D);
+    const size_t er = (size_t)col * Dp + row, ei = (size_t)(Dp + col) * Dp + row;
+    double2& t = gR[(size_t)row * D + col];
+    t = make_double2(t.x + (double)Ghi[er] + (double)Glo[er], t.y + (double)Ghi[ei] + (double)Glo[ei]);
+  }
 }
 
 __global__ void final_state_kernel(const float* Phi, const float* Plo, int Dp, int Rp, double2* rho, int D, int R) {
@@ -305,8 +642,8 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   }
 
   const size_t smem = sg::kSmemBytes;
-  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
   int cur = 0;   // B[2cur], B[2cur+1] hold the current stage input
   for (int step = 0; step < d->n_steps; ++step) {
@@ -314,7 +651,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
       a.stage = s;
       a.Bc[0] = B[2 * cur]; a.Bc[1] = B[2 * cur + 1];
       a.Bn[0] = B[2 * (cur ^ 1)]; a.Bn[1] = B[2 * (cur ^ 1) + 1];
-      rsp::gemm_kernel<false><<<MT * NT, sg::kThreads, smem, st>>>(a);
+      rsp::gemm_kernel<0><<<MT * NT, sg::kThreads, smem, st>>>(a);
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
       cur ^= 1;
@@ -324,7 +661,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
       const int slot = (step + 1) / obs_every - 1;
       ao.Bc[0] = B[2 * cur]; ao.Bc[1] = B[2 * cur + 1];
       ao.obs = d->obs_out + (size_t)slot * d->n_rhs * d->n_obs * 2;
-      rsp::gemm_kernel<true><<<ao.KS * MTo * NT, sg::kThreads, smem, st>>>(ao);
+      rsp::gemm_kernel<1><<<ao.KS * MTo * NT, sg::kThreads, smem, st>>>(ao);
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
     }
@@ -334,6 +671,232 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
                                                                      reinterpret_cast<double2*>(d->rho), D, d->n_rhs);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
+  count_launch(launches);
+  return LIME_OK;
+}
+
+// ---------------------------------------------------------------- discrete adjoint (tensor cores)
+namespace {
+
+struct RadjLayout {
+  int D, Dp, Rp, W, KC, MT, NT, KCg, NTg;
+  size_t apiece, bpiece, state, gapiece, gbpiece, gacc, et, rows;
+  size_t total;
+};
+
+RadjLayout radj_layout(int n, int R, int S, int n_obs) {
+  RadjLayout l;
+  rsp_dims(n, R, l.D, l.Dp, l.Rp, l.W, l.KC, l.MT, l.NT);
+  l.KCg = 8 * l.Rp / sg::kCK;
+  l.NTg = 2 * l.Dp / 128;
+  l.apiece = (size_t)l.MT * l.KC * sg::kPiece;
+  l.bpiece = (size_t)l.NT * l.KC * sg::kPiece;
+  l.state = (size_t)l.W * l.Dp * sizeof(float);
+  l.gapiece = (size_t)l.MT * l.KCg * sg::kPiece;
+  l.gbpiece = (size_t)l.NTg * l.KCg * sg::kPiece;
+  l.gacc = (size_t)2 * l.Dp * l.Dp * sizeof(float);
+  l.et = (((size_t)n_obs * l.D * sizeof(float2)) + 1023) / 1024 * 1024;
+  l.rows = (((size_t)3 * l.MT * 128 * sizeof(float) + (size_t)l.Dp * sizeof(float)) + 1023) / 1024 * 1024;
+  // A pieces of L and L^dag, B ping-pong, state hi/lo/acc, stage inputs of
+  // the segment (4 S + 1), adjoint hi/lo/acc, adjoint stage inputs (4),
+  // gradient A and B pieces, gradient accumulator hi/lo, Et, row scales
+  l.total = 6 * l.apiece + 4 * l.bpiece + 3 * l.state + (4 * (size_t)S + 1) * l.state + 3 * l.state +
+            4 * l.state + 3 * l.gapiece + 2 * l.gbpiece + 2 * l.gacc + l.et + l.rows + 4096;
+  return l;
+}
+
+}  // namespace
+
+extern "C" size_t lime_redfield_adjoint_split_workspace(int32_t n, int32_t n_rhs, int32_t seg_steps, int32_t n_obs) {
+  if (n <= 0 || n_rhs <= 0 || seg_steps <= 0 || n_obs < 0) return 0;
+  return radj_layout(n, n_rhs, seg_steps, n_obs).total;
+}
+
+extern "C" int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d, void* stream) {
+  if (!d || d->n <= 0 || d->n_rhs <= 0 || d->seg_steps <= 0 || d->step0 < 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (!d->R || !d->ckpt || !d->lam || !d->grad_R || !d->workspace || !d->status) return LIME_ERR_ARG;
+  if (d->n_obs > 0 && (!d->obs_ops || !d->obs_grad)) return LIME_ERR_ARG;
+  if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60 || d->margin_log2 < 0 || d->margin_log2 > 30) return LIME_ERR_ARG;
+  if ((int64_t)d->n * d->n > 46340) return LIME_ERR_UNSUPPORTED;
+  const int S = d->seg_steps, R = d->n_rhs, n = d->n, n_obs = d->n_obs;
+  const RadjLayout L = radj_layout(n, R, S, n_obs);
+  if (d->workspace_bytes < L.total) return LIME_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int D = L.D, Dp = L.Dp, Rp = L.Rp;
+  const size_t stf = (size_t)L.W * Dp;   // floats of one state array
+  uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
+  uint8_t* AL[3];
+  uint8_t* ALH[3];
+  for (int i = 0; i < 3; ++i) { AL[i] = w; w += L.apiece; }
+  for (int i = 0; i < 3; ++i) { ALH[i] = w; w += L.apiece; }
+  uint8_t* B[4];
+  for (int i = 0; i < 4; ++i) { B[i] = w; w += L.bpiece; }
+  float* Phi = reinterpret_cast<float*>(w); w += L.state;
+  float* Plo = reinterpret_cast<float*>(w); w += L.state;
+  float* Acc = reinterpret_cast<float*>(w); w += L.state;
+  float* ys = reinterpret_cast<float*>(w); w += (4 * (size_t)S + 1) * L.state;   // [S][4] + after
+  float* Lhi = reinterpret_cast<float*>(w); w += L.state;
+  float* Llo = reinterpret_cast<float*>(w); w += L.state;
+  float* LAcc = reinterpret_cast<float*>(w); w += L.state;
+  float* ast = reinterpret_cast<float*>(w); w += 4 * L.state;                     // a_1..a_4
+  uint8_t* GA[3];
+  for (int i = 0; i < 3; ++i) { GA[i] = w; w += L.gapiece; }
+  uint8_t* GB[2];
+  for (int i = 0; i < 2; ++i) { GB[i] = w; w += L.gbpiece; }
+  float* Ghi = reinterpret_cast<float*>(w); w += L.gacc;
+  float* Glo = reinterpret_cast<float*>(w); w += L.gacc;
+  float2* EtF = reinterpret_cast<float2*>(w); w += L.et;
+  float* rows = reinterpret_cast<float*>(w); w += L.rows;
+  unsigned* lmax = reinterpret_cast<unsigned*>(w);
+  int* sl = reinterpret_cast<int*>(w + 16);
+  float* rinvL = rows;
+  float* rinvLH = rows + (size_t)L.MT * 128;
+  float* rinvG = rows + (size_t)2 * L.MT * 128;
+  float* cinvG = rows + (size_t)3 * L.MT * 128;
+  const float* after = ys + (size_t)4 * S * stf;
+  int64_t launches = 0;
+
+  // operands: L and L^dag pieces, Et, zeroed adjoint arrays and accumulator
+  rsp::convert_rows_kernel<<<Dp, 256, 0, st>>>(reinterpret_cast<const double2*>(d->R), 0, n, D, D, Dp, L.KC, AL[0],
+                                              AL[1], AL[2], rinvL);
+  LIME_CUDA_TRY(cudaGetLastError());
+  rsp::convert_rows_kernel<<<Dp, 256, 0, st>>>(reinterpret_cast<const double2*>(d->R), 2, n, D, D, Dp, L.KC, ALH[0],
+                                              ALH[1], ALH[2], rinvLH);
+  LIME_CUDA_TRY(cudaGetLastError());
+  launches += 2;
+  if (n_obs > 0) {
+    rsp::adj_et_kernel<<<(n_obs * D + 255) / 256, 256, 0, st>>>(reinterpret_cast<const double2*>(d->obs_ops), n_obs,
+                                                               n, EtF);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+  }
+  LIME_CUDA_TRY(cudaMemsetAsync(Lhi, 0, 3 * L.state + 4 * L.state, st));
+  LIME_CUDA_TRY(cudaMemsetAsync(Ghi, 0, 2 * L.gacc, st));
+  LIME_CUDA_TRY(cudaMemsetAsync(lmax, 0, 16, st));
+
+  // ---- recompute the segment from the checkpoint, storing every stage input
+  rsp::StageArgs a{};
+  a.Dp = Dp; a.W = L.W; a.KC = L.KC; a.MT = L.MT; a.NT = L.NT; a.Rp = Rp; a.R = R;
+  a.KS = 1; a.groups_per_split = L.KC / sg::kGroup;
+  a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
+  a.sb = ldexpf(1.f, d->scale_b_log2);
+  a.c_half = (float)(d->dt / 2.0);
+  a.c_full = (float)d->dt;
+  a.c_sixth = (float)(d->dt / 6.0);
+  a.c_sixth_lo = (float)(d->dt / 6.0 - (double)a.c_sixth);
+  a.A[0] = AL[0]; a.A[1] = AL[1]; a.A[2] = AL[2];
+  a.row_inv = rinvL;
+  a.Phi = Phi; a.Plo = Plo; a.Acc = Acc;
+  a.status = d->status;
+  a.max_wait = 1u << 26;
+  a.a_bytes = L.apiece; a.b_bytes = L.bpiece; a.st_floats = stf;
+  a.Bn[0] = B[0]; a.Bn[1] = B[1];
+  a.ystore = ys;
+  const int ib = (int)((stf / 8 + 255) / 256);
+  rsp::init_state_kernel<<<ib < 65535 ? ib : 65535, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->ckpt), D, R);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  const size_t smem = sg::kSmemBytes;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int cur = 0;
+  for (int step = 0; step < S; ++step) {
+    for (int s = 0; s < 4; ++s) {
+      a.stage = s;
+      a.Bc[0] = B[2 * cur]; a.Bc[1] = B[2 * cur + 1];
+      a.Bn[0] = B[2 * (cur ^ 1)]; a.Bn[1] = B[2 * (cur ^ 1) + 1];
+      a.ystore = s < 3 ? ys + ((size_t)step * 4 + s + 1) * stf : ys + (size_t)(step + 1) * 4 * stf;
+      rsp::gemm_kernel<0><<<L.MT * L.NT, sg::kThreads, smem, st>>>(a);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+      cur ^= 1;
+    }
+  }
+
+  // ---- backward over the steps
+  rsp::StageArgs b = a;
+  b.ystore = nullptr;
+  b.A[0] = ALH[0]; b.A[1] = ALH[1]; b.A[2] = ALH[2];
+  b.row_inv = rinvLH;
+  b.Lhi = Lhi; b.Llo = Llo; b.LAcc = LAcc;
+  b.sl_exp = sl;
+  rsp::StageArgs gg = a;   // the gradient GEMM: A = adjoint stage inputs, B = stage inputs
+  gg.ystore = nullptr;
+  gg.KC = L.KCg; gg.MT = L.MT; gg.NT = L.NTg;
+  gg.A[0] = GA[0]; gg.A[1] = GA[1]; gg.A[2] = GA[2];
+  gg.Bc[0] = GB[0]; gg.Bc[1] = GB[1];
+  gg.row_inv = rinvG;
+  gg.a_bytes = L.gapiece; gg.b_bytes = L.gbpiece; gg.st_floats = (size_t)2 * Dp * Dp;
+  gg.Ghi = Ghi; gg.Glo = Glo;
+  gg.col_inv = cinvG;
+  gg.inv_sb = 1.f;   // the B operand is scaled per column (col_inv)
+  const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  const float dt = (float)d->dt;
+  LIME_CUDA_TRY(cudaGetLastError());
+  rsp::adj_lam_in_kernel<<<(int)((((size_t)R * D) + 255) / 256 < 65535 ? (((size_t)R * D) + 255) / 256 : 65535), 256,
+                           0, st>>>(reinterpret_cast<const double2*>(d->lam), D, R, Dp, Rp, Lhi, Llo);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  const int sb_blocks = (int)(((size_t)Rp * (Dp / 8) + 255) / 256);
+  const int eb = (int)((stf / 8 + 255) / 256);
+  for (int step = S - 1; step >= 0; --step) {
+    const int gstep = d->step0 + step;
+    const double2* g = nullptr;
+    if (n_obs > 0 && ((gstep + 1) % obs_every) == 0) {
+      const int slot = (gstep + 1) / obs_every - 1;
+      if (slot < d->n_slots) g = reinterpret_cast<const double2*>(d->obs_grad) + (size_t)slot * R * n_obs;
+    }
+    const float* rho_after = step + 1 < S ? ys + (size_t)(step + 1) * 4 * stf : after;
+    rsp::adj_src_kernel<<<sb_blocks < 65535 ? sb_blocks : 65535, 256, 0, st>>>(Lhi, Llo, D, R, Dp, Rp, EtF, n_obs,
+                                                                               g, lmax);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+    if (g != nullptr && d->grad_obs != nullptr) {
+      rsp::adj_grad_obs_kernel<<<(n_obs * D + 255) / 256, 256, 0, st>>>(rho_after, g, n_obs, n, R, Dp, Rp,
+                                                                       reinterpret_cast<double2*>(d->grad_obs));
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+    }
+    rsp::adj_scale_kernel<<<1, 1, 0, st>>>(lmax, sl, dt / 2.f, d->margin_log2);
+    LIME_CUDA_TRY(cudaGetLastError());
+    b.anext = ast + 3 * stf;
+    b.Bn[0] = B[0]; b.Bn[1] = B[1];
+    rsp::adj_start_kernel<<<eb < 65535 ? eb : 65535, 256, 0, st>>>(b, dt / 6.f);
+    LIME_CUDA_TRY(cudaGetLastError());
+    launches += 2;
+    int c2 = 0;
+    for (int i = 4; i >= 1; --i) {
+      b.adj_i = i;
+      b.Bc[0] = B[2 * c2]; b.Bc[1] = B[2 * c2 + 1];
+      b.Bn[0] = B[2 * (c2 ^ 1)]; b.Bn[1] = B[2 * (c2 ^ 1) + 1];
+      b.anext = i > 1 ? ast + (size_t)(i - 2) * stf : nullptr;
+      b.c_l = i == 2 ? dt / 6.f : dt / 3.f;
+      b.c_y = i == 4 ? dt : dt / 2.f;
+      rsp::gemm_kernel<2><<<L.MT * L.NT, sg::kThreads, smem, st>>>(b);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+      c2 ^= 1;
+    }
+    // generator gradient of the step: sum_i a_i y_i^dag
+    rsp::adj_g_convert_a_kernel<<<Dp, 256, 0, st>>>(ast, stf, Dp, Rp, L.KCg, GA[0], GA[1], GA[2], rinvG);
+    LIME_CUDA_TRY(cudaGetLastError());
+    rsp::adj_g_convert_b_kernel<<<Dp, 256, 0, st>>>(ys + (size_t)step * 4 * stf, stf, Dp, Rp, L.KCg, GB[0], GB[1],
+                                                    cinvG);
+    LIME_CUDA_TRY(cudaGetLastError());
+    rsp::gemm_kernel<3><<<L.MT * L.NTg, sg::kThreads, smem, st>>>(gg);
+    LIME_CUDA_TRY(cudaGetLastError());
+    launches += 3;
+  }
+  rsp::adj_lam_out_kernel<<<(int)((((size_t)R * D) + 255) / 256 < 65535 ? (((size_t)R * D) + 255) / 256 : 65535), 256,
+                            0, st>>>(Lhi, Llo, D, R, Dp, Rp, reinterpret_cast<double2*>(d->lam));
+  LIME_CUDA_TRY(cudaGetLastError());
+  const size_t tot = (size_t)D * D;
+  rsp::adj_g_final_kernel<<<(int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535), 256, 0, st>>>(
+      Ghi, Glo, D, Dp, reinterpret_cast<double2*>(d->grad_R));
+  LIME_CUDA_TRY(cudaGetLastError());
+  launches += 2;
   count_launch(launches);
   return LIME_OK;
 }

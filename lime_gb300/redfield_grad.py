@@ -16,7 +16,8 @@ The reference has no gradients; the forward computation is that of
   ``lime_redfield_assemble_adjoint_f64``;
 * the RK4 time loop runs in the library's FP64 or tensor-core propagators,
   checkpointed every ``checkpoint`` steps, and its discrete adjoint in
-  ``lime_redfield_adjoint_f64`` (backward-in-time RK4 with L^dag and the
+  ``lime_redfield_adjoint_f64`` or, on the tensor cores,
+  ``lime_redfield_adjoint_split`` (backward-in-time RK4 with L^dag and the
   generator gradient sum_i a_i y_i^dag).
 """
 from __future__ import annotations
@@ -116,14 +117,16 @@ class _Propagate(torch.autograd.Function):
         obs = torch.cat(parts, 1) if parts else torch.zeros((rho.shape[0], 0, E.shape[0]), dtype=CDT,
                                                            device=rho.device)
         ctx.save_for_backward(R.detach(), E, *ckpts)
-        ctx.cfg = (float(dt), int(n_steps), int(obs_every), int(checkpoint))
+        ctx.cfg = (float(dt), int(n_steps), int(obs_every), int(checkpoint), precision)
         return obs
 
     @staticmethod
     def backward(ctx, g):
-        lib = nat.require_device()
         R, E, *ckpts = ctx.saved_tensors
-        dt, n_steps, obs_every, checkpoint = ctx.cfg
+        if ctx.cfg[4] == 'split':
+            return _backward_split(R, E, ckpts, g, *ctx.cfg[:4])
+        lib = nat.require_device()
+        dt, n_steps, obs_every, checkpoint = ctx.cfg[:4]
         B, n = ckpts[0].shape[0], ckpts[0].shape[-1]
         D = n * n
         dev = R.device
@@ -151,6 +154,58 @@ class _Propagate(torch.autograd.Function):
         return gR, g_r0, gE, None, None, None, None, None
 
 
+def _backward_split(R, E, ckpts, g, dt, n_steps, obs_every, checkpoint, max_retries=3):
+    """The backward pass on the tensor cores (lime_redfield_adjoint_split),
+    segment by segment from the last; a segment whose adjoint operands left
+    their fixed-point range is repeated with a 4x larger margin (a smaller
+    power-of-two scale of the adjoint stage inputs) or, for the stored
+    states, a 4x smaller state scale."""
+    lib = nat.require_device()
+    B, n = ckpts[0].shape[0], ckpts[0].shape[-1]
+    D = n * n
+    dev = R.device
+    n_obs = E.shape[0]
+    gsrc = g.to(CDT).permute(1, 0, 2).contiguous()           # [slot][rhs][obs]
+    lam = torch.zeros((B, D), dtype=CDT, device=dev)
+    gR = torch.zeros((D, D), dtype=CDT, device=dev)
+    gE = torch.zeros((n_obs, n, n), dtype=CDT, device=dev)
+    segs = _segments(n_steps, checkpoint)
+    wsb = int(lib.lime_redfield_adjoint_split_workspace(n, B, max(m for _, m in segs), n_obs))
+    ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
+    aligned = (ws.data_ptr() + 1023) // 1024 * 1024
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    for (s0, m), ck in reversed(list(zip(segs, ckpts))):
+        P = ck.reshape(B, D).contiguous()
+        pmax = float(torch.view_as_real(P).abs().max().item())
+        sb = int(np.floor(np.log2(8192.0 / (1.25 * pmax)))) if pmax > 0 else 0
+        margin = 0
+        for attempt in range(max_retries + 1):
+            lam_t, gR_t, gE_t = lam.clone(), torch.zeros_like(gR), torch.zeros_like(gE)
+            status.zero_()
+            d = nat.RedfieldAdjointSplitDesc()
+            d.n, d.n_rhs, d.seg_steps, d.step0 = n, B, m, s0
+            d.n_obs, d.obs_every, d.n_slots = n_obs, obs_every, gsrc.shape[0]
+            d.scale_b_log2, d.margin_log2 = max(-60, min(60, sb)), margin
+            d.dt = dt
+            d.R, d.ckpt, d.lam = R.data_ptr(), P.data_ptr(), lam_t.data_ptr()
+            if n_obs:
+                d.obs_ops, d.obs_grad = E.data_ptr(), gsrc.data_ptr()
+            d.grad_R, d.grad_obs = gR_t.data_ptr(), gE_t.data_ptr()
+            d.workspace, d.workspace_bytes = aligned, wsb
+            d.status = status.data_ptr()
+            nat.check(lib.lime_redfield_adjoint_split(d, engine._stream_ptr()), 'lime_redfield_adjoint_split')
+            flags = int(status.item())
+            if flags & nat.LIME_FLAG_RANGE and attempt < max_retries:
+                margin += 2
+                sb -= 2
+                continue
+            if flags:
+                raise nat.KernelFlagError(flags, 'lime_redfield_adjoint_split')
+            break
+        lam, gR, gE = lam_t, gR + gR_t, gE + gE_t
+    return gR, lam.reshape(B, n, n), gE, None, None, None, None, None
+
+
 def redfield_observables(H, a_ops, spectrum, rho0, e_ops, dt: float, n_steps: int, obs_every: int = 1,
                          checkpoint: int = 64, precision: str = 'fp64'):
     """<E_o>(t) = Tr(E_o rho(t)) of the Bloch-Redfield evolution of ``rho0``,
@@ -162,8 +217,9 @@ def redfield_observables(H, a_ops, spectrum, rho0, e_ops, dt: float, n_steps: in
     (n, n) or (B, n, n) and ``e_ops`` (n_obs, n, n) in the site basis.
     Returns (B, n_steps // obs_every, n_obs) complex128, observable k after
     step (k + 1) obs_every - 1 (the reference's timing, t = (k+1) dt for
-    obs_every = 1).  ``precision='split'`` runs the forward on the tensor
-    cores; the backward pass is FP64.  ``checkpoint`` must be a multiple of
+    obs_every = 1).  ``precision='split'`` runs the forward and the backward
+    pass on the tensor cores (lime_redfield_rk4_split,
+    lime_redfield_adjoint_split).  ``checkpoint`` must be a multiple of
     ``obs_every``.
     """
     if precision not in ('fp64', 'split'):

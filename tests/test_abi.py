@@ -61,6 +61,7 @@ def test_null_descriptor_rejected(lib):
     assert lib.lime_redfield_assemble_f64(None, None) == -1
     assert lib.lime_redfield_assemble_adjoint_f64(None, None) == -1
     assert lib.lime_redfield_adjoint_f64(None, None) == -1
+    assert lib.lime_redfield_adjoint_split(None, None) == -1
 
 
 def test_stream_descriptor_validation(lib):
@@ -139,6 +140,7 @@ def _c_layout(struct_name, fields):
     ('LimeRedfieldAssembleDesc', 'RedfieldAssembleDesc'),
     ('LimeRedfieldAssembleAdjointDesc', 'RedfieldAssembleAdjointDesc'),
     ('LimeRedfieldAdjointDesc', 'RedfieldAdjointDesc'),
+    ('LimeRedfieldAdjointSplitDesc', 'RedfieldAdjointSplitDesc'),
     ('LimeRedfieldSplitDesc', 'RedfieldSplitDesc'),
     ('LimeLindbladStreamDesc', 'LindbladStreamDesc'),
     ('LimeLindbladAdjointStreamDesc', 'AdjointStreamDesc'),

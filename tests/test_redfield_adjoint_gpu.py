@@ -126,9 +126,44 @@ def test_redfield_gradients_vs_torch_autograd_and_finite_differences():
             assert abs(fd - g) <= 1e-5 * max(abs(g), 1e-3 * max(x.abs().max().item() for x in g_lib)), (pi, j, fd, g)
 
 
-def test_redfield_gradients_split_forward():
-    """The tensor-core forward (FP64 backward) gives the FP64 gradients to
-    1e-5 relative."""
+# The tensor-core backward's own outputs (the generator gradient G, the
+# gradient of the initial states and of the eigenbasis observables) agree
+# with the FP64 backward to ~1e-7 of their largest element
+# (test_redfield_split_adjoint_raw_outputs).  The parameter gradients are
+# that G contracted with dL/dtheta through the assembly, the spectral factors
+# and the eigenvector derivative of eigh(H) (terms in 1 / (E_a - E_b)),
+# sums of both signs that are much smaller than their terms: the ~1e-7
+# relative error of G reaches them amplified, measured 1.1e-5 relative on the
+# 6-site chain.  Bar for the split path's parameter gradients: 3e-5.
+SPLIT_PARAM_TOL = 3e-5
+
+
+def test_redfield_split_adjoint_raw_outputs():
+    """G, dl/drho0 and dl/dE of the tensor-core backward against the FP64
+    backward, over 1, 3, 20 and 60 steps (one and two checkpoint segments)."""
+    from lime_gb300.redfield import redfield_tensor
+    from lime_gb300.redfield_grad import _Propagate
+    n = 6
+    rw = chains.redfield_chain(n=n, n_rhs=2, cfg=5)
+    R, evecs = redfield_tensor(rw['H'], rw['a_ops'], rw['spectra'])
+    V = torch.as_tensor(evecs, dtype=CDT, device='cuda')
+    r0 = V.mH @ torch.as_tensor(rw['rho0'], dtype=CDT, device='cuda') @ V
+    E = torch.stack([V.mH @ torch.as_tensor(e, device='cuda') @ V for e in chains.population_ops(n)])
+    for steps, ck in ((1, 1), (3, 3), (20, 10), (60, 30)):
+        out = {}
+        for prec in ('fp64', 'split'):
+            leaves = [x.clone().requires_grad_(True) for x in (R.R, r0, E)]
+            obs = _Propagate.apply(*leaves, 0.05, steps, 1, ck, prec)
+            g = torch.tensor(np.random.default_rng(1).normal(size=tuple(obs.shape)), device='cuda').to(CDT)
+            (obs.conj() * g).real.sum().backward()
+            out[prec] = [x.grad for x in leaves]
+        for a, b in zip(out['split'], out['fp64']):
+            assert ((a - b).abs().max() / b.abs().max()).item() < 1e-6, steps
+
+
+def test_redfield_gradients_split():
+    """The tensor-core forward and backward against the FP64 gradients
+    (SPLIT_PARAM_TOL relative)."""
     n, steps, obs_every, ckpt = 6, 60, 3, 30
     m = _model(n, 12)
     weights = torch.tensor(m['rng'].normal(size=(2, steps // obs_every, n)), device='cuda')
@@ -136,4 +171,22 @@ def test_redfield_gradients_split_forward():
     _, g64 = _grads(lambda *p: _loss_lib(m, *p, weights, steps, obs_every, ckpt), params)
     _, gsp = _grads(lambda *p: _loss_lib(m, *p, weights, steps, obs_every, ckpt, 'split'), params)
     for a, b in zip(gsp, g64):
-        assert (a - b).abs().max().item() <= 1e-5 * max(b.abs().max().item(), 1e-300)
+        assert (a - b).abs().max().item() <= SPLIT_PARAM_TOL * max(b.abs().max().item(), 1e-300)
+
+
+def test_redfield_split_adjoint_larger_block():
+    """The tensor-core backward on a 12-site chain (Liouville dimension 144,
+    padded to 256) with 70 right-hand sides (two column tiles) and uneven
+    segments, against the FP64 backward."""
+    n, steps, obs_every, ckpt = 12, 50, 1, 20
+    m = _model(n, 13)
+    rng = m['rng']
+    psi = rng.normal(size=(70, n)) + 1j * rng.normal(size=(70, n))
+    psi /= np.linalg.norm(psi, axis=1, keepdims=True)
+    m['rho0'] = torch.as_tensor(np.einsum('bi,bj->bij', psi, psi.conj()), device='cuda')
+    weights = torch.tensor(rng.normal(size=(70, steps // obs_every, n)), device='cuda')
+    params = [m['eps'], m['J'], m['s'], m['lam']]
+    _, g64 = _grads(lambda *p: _loss_lib(m, *p, weights, steps, obs_every, ckpt), params)
+    _, gsp = _grads(lambda *p: _loss_lib(m, *p, weights, steps, obs_every, ckpt, 'split'), params)
+    for a, b in zip(gsp, g64):
+        assert (a - b).abs().max().item() <= SPLIT_PARAM_TOL * max(b.abs().max().item(), 1e-300)
