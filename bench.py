@@ -70,6 +70,8 @@ def parse():
     p.add_argument('--redfield-adjoint-only', action='store_true',
                    help='run only the Redfield adjoint/forward leg and print its JSON')
     p.add_argument('--no-redfield-adjoint', action='store_true')
+    p.add_argument('--redfield-adjoint-steps', type=int, default=128)
+    p.add_argument('--redfield-adjoint-checkpoint', type=int, default=64)
     p.add_argument('--adjoint-batch', type=int, default=256)
     p.add_argument('--ragged-batch', type=int, default=1024)
     p.add_argument('--ragged-sizes', default='8,16,32,64,128,256',
@@ -198,7 +200,8 @@ def gpu_arm(args, rank, world, local):
         return
     if args.redfield_adjoint_only:
         if rank == 0:
-            print(json.dumps(redfield_adjoint_leg(torch, dev)))
+            print(json.dumps(redfield_adjoint_leg(torch, dev, steps=args.redfield_adjoint_steps,
+                                                  checkpoint=args.redfield_adjoint_checkpoint)))
         return
     if args.ragged_only:
         if rank == 0:
@@ -295,7 +298,8 @@ def gpu_arm(args, rank, world, local):
         errors = full_horizon_leg(torch, dev)
     radj = None
     if not args.no_redfield_adjoint and single:
-        radj = redfield_adjoint_leg(torch, dev)
+        radj = redfield_adjoint_leg(torch, dev, steps=args.redfield_adjoint_steps,
+                                    checkpoint=args.redfield_adjoint_checkpoint)
     cpu = None
     if not args.no_cpu and rank == 0 and world == 1:
         from oracle import pool

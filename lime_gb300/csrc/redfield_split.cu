@@ -303,48 +303,55 @@ __global__ void adj_lam_out_kernel(const float* Lhi, const float* Llo, int D, in
 }
 
 // lam += Et^dag g (the observables recorded after the step, g [R][n_obs]
-// complex128, or none) and max |lam| of the step; one thread per (column
-// r, run of 8 rows d), both components
+// complex128, or none) and max |lam| of the step.  One thread per row d and
+// a chunk of 8 right-hand sides: Et[o][d] is read once per chunk
+// (coalesced across the warp's rows) and the chunk's g from shared memory.
 __global__ void adj_src_kernel(float* Lhi, float* Llo, int D, int R, int Dp, int Rp, const float2* EtF, int n_obs,
                                const double2* g, unsigned* lmax) {
-  const size_t runs = (size_t)Dp / 8, total = (size_t)Rp * runs;
+  extern __shared__ float2 gs[];   // [8][n_obs]
+  const int chunks = Rp / 8;
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
   float mx = 0.f;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
-    const int r = (int)(q / runs), d0 = (int)(q % runs) * 8;
-    const size_t er = (size_t)r * Dp + d0, ei = (size_t)(Rp + r) * Dp + d0;
-    float hr[8], hi[8];
-    sg::ld8(Lhi + er, hr);
-    sg::ld8(Lhi + ei, hi);
-    if (g != nullptr && r < R) {
-      float sr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, si[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int ch = blockIdx.y; ch < chunks; ch += gridDim.y) {
+    const int r0 = ch * 8;
+    if (g != nullptr) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < 8 * n_obs; q += blockDim.x) {
+        const int rr = r0 + q / n_obs, o = q % n_obs;
+        const double2 v = rr < R ? g[(size_t)rr * n_obs + o] : make_double2(0.0, 0.0);
+        gs[q] = make_float2((float)v.x, (float)v.y);
+      }
+      __syncthreads();
+    }
+    if (d >= Dp) continue;
+    float sr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, si[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (g != nullptr && d < D) {
       for (int o = 0; o < n_obs; ++o) {
-        const double2 gv = g[(size_t)r * n_obs + o];
-        const float gr = (float)gv.x, gi = (float)gv.y;
+        const float2 et = EtF[(size_t)o * D + d];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-          if (d0 + i < D) {
-            // conj(Et) g = (er gr + ei gi) + i (er gi - ei gr)
-            const float2 et = EtF[(size_t)o * D + d0 + i];
-            sr[i] = __fmaf_rn(et.x, gr, __fmaf_rn(et.y, gi, sr[i]));
-            si[i] = __fmaf_rn(et.x, gi, __fmaf_rn(-et.y, gr, si[i]));
-          }
+          // conj(Et) g = (er gr + ei gi) + i (er gi - ei gr)
+          const float2 gv = gs[i * n_obs + o];
+          sr[i] = __fmaf_rn(et.x, gv.x, __fmaf_rn(et.y, gv.y, sr[i]));
+          si[i] = __fmaf_rn(et.x, gv.y, __fmaf_rn(-et.y, gv.x, si[i]));
         }
       }
-      float lr[8], li[8];
-      sg::ld8(Llo + er, lr);
-      sg::ld8(Llo + ei, li);
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        hr[i] = rk4_final_f32(hr[i], 0.f, sr[i], 1.f, 0.f, lr[i]);
-        hi[i] = rk4_final_f32(hi[i], 0.f, si[i], 1.f, 0.f, li[i]);
-      }
-      sg::st8(Lhi + er, hr);
-      sg::st8(Llo + er, lr);
-      sg::st8(Lhi + ei, hi);
-      sg::st8(Llo + ei, li);
     }
 #pragma unroll
-    for (int i = 0; i < 8; ++i) mx = fmaxf(mx, fmaxf(fabsf(hr[i]), fabsf(hi[i])));
+    for (int i = 0; i < 8; ++i) {
+      const size_t er = (size_t)(r0 + i) * Dp + d, ei = (size_t)(Rp + r0 + i) * Dp + d;
+      float hr = Lhi[er], hi = Lhi[ei];
+      if (g != nullptr && d < D && r0 + i < R) {
+        float lr = Llo[er], li = Llo[ei];
+        hr = rk4_final_f32(hr, 0.f, sr[i], 1.f, 0.f, lr);
+        hi = rk4_final_f32(hi, 0.f, si[i], 1.f, 0.f, li);
+        Lhi[er] = hr;
+        Llo[er] = lr;
+        Lhi[ei] = hi;
+        Llo[ei] = li;
+      }
+      mx = fmaxf(mx, fmaxf(fabsf(hr), fabsf(hi)));
+    }
   }
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(lmax, __float_as_uint(mx));
@@ -388,23 +395,49 @@ __global__ void adj_start_kernel(StageArgs a, float dt6) {
 }
 
 // grad_E[o][b][a] += sum_r g[r][o] conj(rho[(a, b)][r]) for the observables
-// recorded after the step (rho planar [W][Dp] fp32); one thread per (o, d)
+// recorded after the step (rho planar [W][Dp] fp32).  One thread per row d
+// and a chunk of 8 observables: rho is read once per chunk (coalesced), g
+// for the chunk comes from shared memory.
 __global__ void adj_grad_obs_kernel(const float* rho, const double2* g, int n_obs, int n, int R, int Dp, int Rp,
                                     double2* gE) {
+  constexpr int kRC = 256;          // right-hand sides per shared-memory chunk
+  __shared__ float2 gs[kRC * 8];   // [r][8]
   const int D = n * n;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n_obs * D; e += gridDim.x * blockDim.x) {
-    const int o = e / D, d = e % D;
-    float vr = 0.f, vi = 0.f;
-    for (int r = 0; r < R; ++r) {
-      const double2 gv = g[(size_t)r * n_obs + o];
-      const float pr = rho[(size_t)r * Dp + d], pi = rho[(size_t)(Rp + r) * Dp + d];
-      // g conj(rho) = (gr pr + gi pi) + i (gi pr - gr pi)
-      vr = __fmaf_rn((float)gv.x, pr, __fmaf_rn((float)gv.y, pi, vr));
-      vi = __fmaf_rn((float)gv.y, pr, __fmaf_rn(-(float)gv.x, pi, vi));
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int o0 = blockIdx.y * 8; o0 < n_obs; o0 += gridDim.y * 8) {
+    float vr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vi[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int rc = 0; rc < R; rc += kRC) {
+      const int rn = R - rc < kRC ? R - rc : kRC;
+      __syncthreads();
+      for (int q = threadIdx.x; q < 8 * rn; q += blockDim.x) {
+        const int r = rc + q / 8, o = o0 + q % 8;
+        const double2 v = o < n_obs ? g[(size_t)r * n_obs + o] : make_double2(0.0, 0.0);
+        gs[q] = make_float2((float)v.x, (float)v.y);
+      }
+      __syncthreads();
+      if (d < D) {
+        for (int rr = 0; rr < rn; ++rr) {
+          const int r = rc + rr;
+          const float pr = rho[(size_t)r * Dp + d], pi = rho[(size_t)(Rp + r) * Dp + d];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            // g conj(rho) = (gr pr + gi pi) + i (gi pr - gr pi)
+            const float2 gv = gs[rr * 8 + i];
+            vr[i] = __fmaf_rn(gv.x, pr, __fmaf_rn(gv.y, pi, vr[i]));
+            vi[i] = __fmaf_rn(gv.y, pr, __fmaf_rn(-gv.x, pi, vi[i]));
+          }
+        }
+      }
     }
+    if (d >= D) continue;
     const int ia = d / n, ib = d % n;
-    double2& t = gE[(size_t)o * D + (size_t)ib * n + ia];
-    t = make_double2(t.x + (double)vr, t.y + (double)vi);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (o0 + i < n_obs) {
+        double2& t = gE[(size_t)(o0 + i) * D + (size_t)ib * n + ia];
+        t = make_double2(t.x + (double)vr[i], t.y + (double)vi[i]);
+      }
+    }
   }
 }
 
@@ -839,7 +872,6 @@ extern "C" int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d
                            0, st>>>(reinterpret_cast<const double2*>(d->lam), D, R, Dp, Rp, Lhi, Llo);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
-  const int sb_blocks = (int)(((size_t)Rp * (Dp / 8) + 255) / 256);
   const int eb = (int)((stf / 8 + 255) / 256);
   for (int step = S - 1; step >= 0; --step) {
     const int gstep = d->step0 + step;
@@ -849,13 +881,17 @@ extern "C" int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d
       if (slot < d->n_slots) g = reinterpret_cast<const double2*>(d->obs_grad) + (size_t)slot * R * n_obs;
     }
     const float* rho_after = step + 1 < S ? ys + (size_t)(step + 1) * 4 * stf : after;
-    rsp::adj_src_kernel<<<sb_blocks < 65535 ? sb_blocks : 65535, 256, 0, st>>>(Lhi, Llo, D, R, Dp, Rp, EtF, n_obs,
-                                                                               g, lmax);
+    {
+      const dim3 sg_grid((Dp + 255) / 256, Rp / 8 < 8 ? Rp / 8 : 8);
+      rsp::adj_src_kernel<<<sg_grid, 256, (size_t)8 * (n_obs > 0 ? n_obs : 1) * sizeof(float2), st>>>(
+          Lhi, Llo, D, R, Dp, Rp, EtF, n_obs, g, lmax);
+    }
     LIME_CUDA_TRY(cudaGetLastError());
     ++launches;
     if (g != nullptr && d->grad_obs != nullptr) {
-      rsp::adj_grad_obs_kernel<<<(n_obs * D + 255) / 256, 256, 0, st>>>(rho_after, g, n_obs, n, R, Dp, Rp,
-                                                                       reinterpret_cast<double2*>(d->grad_obs));
+      const dim3 go_grid((D + 255) / 256, (n_obs + 7) / 8);
+      rsp::adj_grad_obs_kernel<<<go_grid, 256, 0, st>>>(
+          rho_after, g, n_obs, n, R, Dp, Rp, reinterpret_cast<double2*>(d->grad_obs));
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
     }

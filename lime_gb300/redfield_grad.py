@@ -230,9 +230,11 @@ def redfield_observables(H, a_ops, spectrum, rho0, e_ops, dt: float, n_steps: in
     H = torch.as_tensor(H, device=dev)
     A0 = torch.stack([torch.as_tensor(a, device=dev) for a in a_ops]) if isinstance(a_ops, (list, tuple)) \
         else torch.as_tensor(a_ops, device=dev)
-    E, V = torch.linalg.eigh(H)
-    E = E.to(torch.float64)
-    Vc = V.to(CDT)
+    # the n x n eigendecomposition runs on the host, as in the reference
+    # (scipy eigh in redfield_tensor); autograd carries the device transfer
+    E, V = torch.linalg.eigh(H.cpu())
+    E = E.to(device=dev, dtype=torch.float64)
+    Vc = V.to(device=dev, dtype=CDT)
     A = Vc.mH @ A0.to(CDT) @ Vc                                    # (K, n, n)
     W = E[:, None] - E[None, :]
     if callable(spectrum):
