@@ -321,10 +321,11 @@ def gpu_arm(args, rank, world, local):
         pk = peaks.get('bf16_tflops_sustained') or 1700.0
         # issued tensor work: per stage 5 fp16 products of the 128x64x128 real block
         issued = 4 * 5 * 2 * 128 * 64 * 128
-        # DRAM traffic per launch: 150.5 KB per instance (ncu capture of 304
-        # instances x 400 steps: 40.8 MB read + 4.9 MB written), scaled by the
-        # instances one full-size launch processes; it does not grow with steps
-        traffic = 150.5e3 * B
+        # DRAM traffic per launch: 185.5 KB per instance (ncu capture of 304
+        # instances x 400 steps: 50.5 MB read + 5.9 MB written: the prepared A
+        # pieces and rho in, rho out), scaled by the instances one full-size
+        # launch processes; it does not grow with steps
+        traffic = 185.5e3 * B
         roof = {'bound': 'tensor', 'achieved': achieved_tf, 'peak': pk, 'unit': 'TFLOP/s',
                 'frac': achieved_tf / pk, 'traffic': traffic,
                 'traffic_source': 'ncu dram__bytes_read+write of a 304-instance launch, '
