@@ -548,80 +548,95 @@ def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k
         torch.cuda.synchronize()
         return out, a.elapsed_time(b) / 1e3
 
-    propagate_vec_split(Rg, r0, dt, 1, e_eb)
-    _, t1 = timed(lambda: propagate_vec_split(Rg, r0, dt, k_split[0], e_eb))
-    _, t2 = timed(lambda: propagate_vec_split(Rg, r0, dt, k_split[1], e_eb))
-    per_step = (t2 - t1) / (k_split[1] - k_split[0])
+    from lime_gb300 import redfield as rfm
+    per_step = {}
+    for prod in ('4m', '3m'):
+        propagate_vec_split(Rg, r0, dt, 1, e_eb, product=prod)
+        _, t1 = timed(lambda: propagate_vec_split(Rg, r0, dt, k_split[0], e_eb, product=prod))
+        _, t2 = timed(lambda: propagate_vec_split(Rg, r0, dt, k_split[1], e_eb, product=prod))
+        per_step[prod] = (t2 - t1) / (k_split[1] - k_split[0])
     (o64, _, r64), t64 = timed(lambda: propagate_vec(Rg, r0, dt, k64, e_eb))
-    (osp, _, rsp), _ = timed(lambda: propagate_vec_split(Rg, r0, dt, k64, e_eb))
+    errs = {}
+    for prod in ('4m', '3m'):
+        (osp, _, rsp), _ = timed(lambda: propagate_vec_split(Rg, r0, dt, k64, e_eb, product=prod))
+        errs[prod] = ((osp - o64).abs().max().item(), (rsp - r64).abs().max().item())
     D = n * n
     stage_flop = 8.0 * D * D * n_rhs          # one complex D x D x R GEMM
-    issued = 5 * stage_flop                   # five fp16 products per real block
+    # issued tensor flops per stage: five fp16 products per real product;
+    # the block form multiplies 4 real D x D x R products, the 3M form 3
+    issued = {'4m': 5 * stage_flop, '3m': 5 * 0.75 * stage_flop}
     pk = peaks.get('bf16_tflops_sustained') or 1700.0
-    split_rate = n_rhs / per_step
+    prod = rfm.SPLIT_PRODUCT
+    split_rate = n_rhs / per_step[prod]
     fp64_rate = n_rhs * k64 / t64
+
+    def entry(p):
+        return {'value': n_rhs / per_step[p], 'ms_per_step': per_step[p] * 1e3,
+                'sample': 'difference of %d- and %d-step runs' % k_split,
+                'max_population_error': errs[p][0], 'max_state_error': errs[p][1],
+                'achieved_algorithmic_tflops': 4 * stage_flop / per_step[p] / 1e12,
+                'achieved_issued_tflops': 4 * issued[p] / per_step[p] / 1e12}
+
     return {'workload': 'Redfield dense superoperator, spin-boson-like exciton chain N=%d '
                         '(Liouville dim %d), Ohmic bath, %d initial density matrices as one '
                         'right-hand-side block' % (n, D, n_rhs),
             'unit': 'instance-steps/s',
-            'split': {'value': split_rate, 'ms_per_step': per_step * 1e3,
-                      'sample': 'difference of %d- and %d-step runs' % k_split},
+            'split': dict(entry(prod), product=prod),
+            'split_4m': entry('4m'), 'split_3m': entry('3m'),
             'fp64_gpu': {'value': fp64_rate, 'ms_per_step': t64 / k64 * 1e3,
                          'sample': '%d RK4 steps' % k64},
             'speedup_vs_fp64_gpu': split_rate / fp64_rate,
-            'split_max_population_error': (osp - o64).abs().max().item(),
-            'split_max_state_error': (rsp - r64).abs().max().item(),
-            'error_sample': 'all %d right-hand sides, %d steps' % (n_rhs, k64),
+            'split_max_population_error': errs[prod][0],
+            'split_max_state_error': errs[prod][1],
+            'error_sample': 'all %d right-hand sides, %d steps (full horizon: full_horizon_errors)'
+                            % (n_rhs, k64),
             'roofline': {'bound': 'tensor', 'unit': 'TFLOP/s',
-                         'achieved_algorithmic': 4 * stage_flop / per_step / 1e12,
-                         'achieved_issued': 4 * issued / per_step / 1e12,
-                         'peak': pk, 'frac_issued': 4 * issued / per_step / 1e12 / pk,
-                         'note': 'per-step time includes the 4 stage launches and one '
-                                 'observable launch'}}
+                         'achieved_algorithmic': 4 * stage_flop / per_step[prod] / 1e12,
+                         'achieved_issued': 4 * issued[prod] / per_step[prod] / 1e12,
+                         'peak': pk, 'frac_issued': 4 * issued[prod] / per_step[prod] / 1e12 / pk,
+                         'note': 'per-step time includes the stage launches and one observable '
+                                 'launch'}}
 
 
 def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_split=40, steps_fp64=2,
                err_steps=200):
     """Uneven batch: 1024 chains with N uniform over {8..256}, three dense
     complex collapse operators each (2000-step workload; samples of steps
-    are timed).  The groups of ``engine.propagate_ragged`` (one batched
-    launch sequence per size, chains of N <= 32 packed block-diagonally on
-    the split path), the sizes on concurrent streams.  The generators are
-    prepared once; CUDA events on the joining stream time the GPU work of a
-    whole call (all sizes), and the split per-step time is the difference of
-    a 20- and a 40-step call (the per-call operand conversion cancels).  The
-    split error on populations is taken over err_steps steps on two chains
-    of every N <= 128 through the public call."""
+    are timed).  The schedule of the split path (one grouped persistent
+    launch per GEMM phase for all sizes, or one launch sequence per size on
+    concurrent streams; tile order; block-diagonal packing of N <= 32) is
+    picked first by the autotuner (``engine.autotune_ragged``, outside the
+    timed region); the groups are prepared once; CUDA events on the main
+    stream time the GPU work of a whole call (all sizes), and the split
+    per-step time is the difference of a 20- and a 40-step call (the
+    per-call operand conversion cancels).  The split error on populations
+    is taken over err_steps steps on two chains of every N <= 128 through
+    the public call."""
     import numpy as np
-    from lime_gb300 import chains, engine
+    from lime_gb300 import chains, engine, tuning
     w = chains.uneven_batch(batch=batch, sizes=sizes, n_steps=steps_split)
     ns = w['ns']
     E = [[chains.population_ops(int(n))[0]] for n in ns]
     main = torch.cuda.current_stream(dev)
-    # the public uneven-batch call's groups (split: chains of N <= 32 packed
-    # block-diagonally, 64 // N to an instance), prepared once per precision
-    prepared = {}
-    for prec in ('split', 'fp64'):
-        prepared[prec] = [(g, torch.cuda.Stream(device=dev)) for g in
-                          engine.ragged_groups(w['H'], w['rho0'], w['c_ops'], E, prec, dev)]
+    cache = tuning.TuneCache(os.path.join(tempfile.gettempdir(), 'lime_gb300_tune_bench.json'))
+    choice, times = engine.autotune_ragged(w['H'], w['rho0'], w['dt'], w['c_ops'], E, precision='split',
+                                           device=dev, cache=cache, force=True)
+    prepared = {
+        'split': engine.ragged_groups(w['H'], w['rho0'], w['c_ops'], E, 'split', dev, pack=choice['pack']),
+        'fp64': engine.ragged_groups(w['H'], w['rho0'], w['c_ops'], E, 'fp64', dev),
+    }
+    sched = {'split': choice, 'fp64': {'mode': 'streams'}}
 
     def run(steps, precision):
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         a.record(main)
-        fins = []
-        for g, st in prepared[precision]:
-            st.wait_stream(main)
-            with torch.cuda.stream(st):
-                fins.append(engine._launch(g.gen, g.rho, w['dt'], steps, g.e_ops, precision=precision,
-                                           defer=True))
-        for _, st in prepared[precision]:
-            main.wait_stream(st)
+        fins = engine.ragged_enqueue(prepared[precision], w['dt'], steps, precision, sched[precision],
+                                     device=dev)
         b.record(main)
         torch.cuda.synchronize()
-        for (_, st), fin in zip(prepared[precision], fins):
-            with torch.cuda.stream(st):
-                fin(True)
+        for fin in fins:
+            fin(True)
         return a.elapsed_time(b) / 1e3
 
     run(1, 'split')   # warm
@@ -637,7 +652,7 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
     args = ([w['H'][i] for i in sub], [w['rho0'][i] for i in sub], w['dt'], err_steps,
             [w['c_ops'][i] for i in sub], [E[i] for i in sub])
     o64, _, _ = engine.propagate_ragged(*args, precision='fp64')
-    osp, _, _ = engine.propagate_ragged(*args, precision='split')
+    osp, _, _ = engine.propagate_ragged(*args, precision='split', schedule=choice)
     err = max(float((x - y).abs().max().item()) for x, y in zip(osp, o64))
     flop = float(sum(256.0 * int(n) ** 3 for n in ns))   # 64 (1 + K) N^3 per instance-step, K = 3
     split_rate = len(ns) / per_step
@@ -650,9 +665,14 @@ def ragged_leg(torch, dev, batch=1024, sizes=(8, 16, 32, 64, 128, 256), steps_sp
                                 % (steps_split // 2, steps_split),
                       'gpu_s_%d_steps' % steps_split: t2,
                       'algorithmic_tflops': flop / per_step / 1e12,
-                      'path': 'streaming tcgen05 GEMMs (Heff rho, L rho L^dag), one launch '
-                              'sequence per size (chains of N <= 32 packed block-diagonally, '
-                              '64 // N to an instance), sizes on concurrent streams'},
+                      'path': 'streaming tcgen05 GEMMs (Heff rho, L rho L^dag); schedule %s'
+                              % json.dumps(choice, sort_keys=True),
+                      'schedule': choice,
+                      'tuning': {'key': tuning.key('lindblad_uneven',
+                                                   engine.uneven_class(w['H'], w['c_ops'], 'split'),
+                                                   'split', tuning.arch_tag(dev)),
+                                 'ms_per_step': {json.dumps(c, sort_keys=True): (None if t is None else t * 1e3)
+                                                 for c, t in zip(engine.UNEVEN_CANDIDATES, times or [])}}},
             'fp64_gpu': {'value': fp64_rate, 'steps': steps_fp64, 'gpu_s': tf},
             'speedup_vs_fp64_gpu': split_rate / fp64_rate,
             'split_max_population_error': err,
@@ -822,12 +842,16 @@ def full_horizon_leg(torch, dev):
     r0 = V.mH @ torch.as_tensor(w['rho0'], dtype=torch.complex128, device=dev) @ V
     Eeb = torch.stack([V.mH @ torch.as_tensor(e, dtype=torch.complex128, device=dev) @ V
                        for e in chains.population_ops(96)])
-    (osp, _, rsp), tsp = clock(lambda: propagate_vec_split((R.R, 96), r0, 0.05, 2000, list(Eeb), obs_every=10))
     (o64, r64), t64 = clock(lambda: fp64_torch.redfield_rk4(R.R, r0, 0.05, 2000, Eeb, obs_every=10))
-    out['redfield_dim9216'] = {'sample': '2 right-hand sides x 2000 steps, 96 populations every 10 steps',
-                               'max_population_error': (osp - o64).abs().max().item(),
-                               'max_state_error': (rsp - r64).abs().max().item(),
-                               'reference': 'PyTorch FP64 RK4', 'split_s': tsp, 'fp64_s': t64}
+    for prod in ('4m', '3m'):
+        (osp, _, rsp), tsp = clock(lambda: propagate_vec_split((R.R, 96), r0, 0.05, 2000, list(Eeb), obs_every=10,
+                                                               product=prod))
+        out['redfield_dim9216' + ('' if prod == '4m' else '_3m')] = {
+            'sample': '2 right-hand sides x 2000 steps, 96 populations every 10 steps',
+            'product': prod,
+            'max_population_error': (osp - o64).abs().max().item(),
+            'max_state_error': (rsp - r64).abs().max().item(),
+            'reference': 'PyTorch FP64 RK4', 'split_s': tsp, 'fp64_s': t64}
     out['bar'] = 'populations <= 1e-6 absolute, correlations <= 1e-6 relative to max |C|'
     return out
 
@@ -857,7 +881,7 @@ def e2e_leg(wl, K, path, dev):
     B = wl['H'].shape[0]
     H = torch.as_tensor(wl['H']).pin_memory()
     g = torch.as_tensor(wl['gamma']).pin_memory()
-    rho0 = wl['rho0']
+    rho0 = torch.as_tensor(wl['rho0']).pin_memory()
     pops = Populations(N_SITES)
     nout = max(1, K // 100)
     sol = Lindblad_solver(H, c_ops=[SiteDephasing(g)], precision=path)
@@ -867,7 +891,7 @@ def e2e_leg(wl, K, path, dev):
     res = sol.evolve(rho0, dt=DT, Nt=K, e_ops=pops, nout=nout, store_states=False)
     torch.cuda.synchronize()
     t = time.perf_counter() - t0
-    h2d = H.numel() * 16 + g.numel() * 8 + rho0.size * 16
+    h2d = H.numel() * 16 + g.numel() * 8 + rho0.numel() * 16
     d2h = res.observables.nbytes + np.asarray(res.rholist).nbytes
     return {'value': B * K / t, 'unit': 'instance-steps/s', 'wall_s': t,
             'h2d_bytes_per_step': h2d / K, 'd2h_bytes_per_step': d2h / K,

@@ -334,6 +334,17 @@ typedef struct {
 size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs, int32_t n_obs);
 int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* stream);
 
+/* The same propagation with the complex product in its 3M form: per stage
+ * the three real products T1 = Lr Sr, T2 = Li Si, T3 = (Lr + Li)(Sr + Si)
+ * (one streaming launch over all three; Yr = T1 - T2, Yi = T3 - T1 - T2
+ * formed from their fp32 two-sum words in an elementwise stage kernel with
+ * the RK4 update), three quarters of the tensor-core products of the block
+ * form.  Same descriptor and semantics as lime_redfield_rk4_split (the sum
+ * operand Sr + Si is held at half the state scale); workspace
+ * lime_redfield_split3_workspace(n, n_rhs, n_obs) bytes, 1024-byte aligned. */
+size_t lime_redfield_split3_workspace(int32_t n, int32_t n_rhs, int32_t n_obs);
+int lime_redfield_rk4_split3(const LimeRedfieldSplitDesc* d, void* stream);
+
 /* The discrete adjoint of lime_redfield_rk4_split over one checkpoint
  * segment, on the tensor cores (no counterpart in the reference): the
  * recursion of lime_redfield_adjoint_f64 with every generator application
@@ -417,6 +428,24 @@ typedef struct {
 
 size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops);
 int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream);
+
+/* An uneven batch: n_groups propagations of the form above (each its own
+ * dimension, operator count, batch, buffers, workspace and status word)
+ * with a common n_steps, dt and obs_every and no drive, run in lockstep:
+ * per RK4 stage ONE persistent launch runs the GEMM 1 tiles of every group
+ * and one the GEMM 2 tiles (a CTA per SM loops over the concatenated tile
+ * list, starting the next tile's operand copies and MMAs while the epilogue
+ * of the previous one runs).  Replaces the per-instance calls of
+ * lime/oqs.py:1590-1688 for instances of different sizes.
+ *   n_ctas    persistent CTAs per launch (0: one per SM)
+ *   order     1: tiles of the groups with the most K chunks per tile first
+ *             (longest first); 0: groups in the given order
+ * Returns LIME_ERR_UNSUPPORTED for n_groups > lime_lindblad_stream_max_groups()
+ * or a driven group.  Range retries are per group, through
+ * lime_lindblad_rk4_stream. */
+int32_t lime_lindblad_stream_max_groups(void);
+int lime_lindblad_rk4_stream_groups(const LimeLindbladStreamDesc* descs, int32_t n_groups, int32_t n_ctas,
+                                    int32_t order, void* stream);
 
 /* Discrete adjoint of the RK4 steps of lime_lindblad_rk4_stream for the
  * chain model (site energies on the diagonal, nearest-neighbour bonds, site

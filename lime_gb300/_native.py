@@ -243,8 +243,13 @@ SIGNATURES = [
     ('lime_redfield_rk4_f64', c_int32, [ctypes.POINTER(RedfieldRK4Desc), c_void_p]),
     ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32, c_int32]),
     ('lime_redfield_rk4_split', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
+    ('lime_redfield_split3_workspace', c_size_t, [c_int32, c_int32, c_int32]),
+    ('lime_redfield_rk4_split3', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_lindblad_stream_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_stream', c_int32, [ctypes.POINTER(LindbladStreamDesc), c_void_p]),
+    ('lime_lindblad_stream_max_groups', c_int32, []),
+    ('lime_lindblad_rk4_stream_groups', c_int32, [ctypes.POINTER(LindbladStreamDesc), c_int32, c_int32, c_int32,
+                                                  c_void_p]),
     ('lime_lindblad_adjoint_stream_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_adjoint_stream', c_int32, [ctypes.POINTER(AdjointStreamDesc), c_void_p]),
     ('lime_noalloc_scratch_bytes', c_size_t, []),

@@ -150,20 +150,90 @@ __device__ __forceinline__ void update8(const Args& a, int b, int jj, int y, con
                     a.b1_bytes - boff, a.status);
 }
 
-// kZ = false: GEMM 1 (X and Y_k rows); kZ = true: GEMM 2 and the stage update.
-template <bool kZ>
-__global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
-  extern __shared__ uint8_t smem_raw[];
-  sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+// The fused epilogue of tile (b, mt, nt), run by the kEpiThreads epilogue
+// threads: kZ = false: GEMM 1 (X rows into Xg, Y_k rows as Y^dag into
+// GEMM 2's B operand); kZ = true: GEMM 2, f and the RK4 stage update.  The
+// finished tile is read through park1(col, row) (one value) and
+// park8(col, row, v) (rows row..row+7).
+template <bool kZ, class P1, class P8>
+__device__ __forceinline__ void fused_epilogue(const Args& a, int b, int mt, int nt, const P1& park1,
+                                               const P8& park8) {
   const int t = threadIdx.x, lane = t & 31;
+  const int u = t - sg::kEpiFirst, ew = u >> 5;
+  const int np = a.np;
+  bool bad = false, range = false;
+  if (!kZ) {
+    // ---- X rows (block 0): the tile columns into Xg, runs of 8 rows
+    const int nlo = lane & 7, glo = lane >> 3;
+#pragma unroll 1
+    for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
+      const int jl = (wi >> 2) * 8 + nlo;
+      const int dl = ((wi & 3) * 4 + glo) * 8;
+      const int R = mt * kBM + dl;
+      const size_t xo = (size_t)b * inst_floats(a) + (size_t)(nt * kBN + jl) * np + R;
+      if (R < np && in_bounds(xo * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status)) {
+        float v[8];
+        park8(jl, dl, v);
+        sg::st8(a.Xg + xo, v);
+      }
+    }
+    // ---- Y_k rows (blocks 1..K): Y^dag into B2, runs of 8 columns of one row
+    const int r = u & 127, o0 = u >> 7;
+    constexpr int kGroups = sg::kEpiThreads / 128;
+    const int R = mt * kBM + r;
+    const int blk = R / np, yrow = R - blk * np;
+    if (blk >= 1 && blk <= a.K) {
+      uint8_t* B20 = a.B2[0] + (size_t)b * a.NT * a.KC2 * kPiece;
+      uint8_t* B21 = a.B2[1] + (size_t)b * a.NT * a.KC2 * kPiece;
+#pragma unroll 1
+      for (int i = 0; i < 16 / kGroups; ++i) {
+        const int cl = 8 * (o0 + kGroups * i);
+        const int jj = nt * kBN + cl;
+        const bool im = jj >= np;
+        const int x = im ? jj - np : jj;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+          // S2[(k-1) np + x][yrow] = conj(Y_k[yrow][x]): real part Yr, imaginary part -Yi
+          const float y = park1(cl + e, r);
+          v[e] = __fmul_rn(im ? -y : y, a.sy);
+          range |= !(fabsf(v[e]) <= sg::kBMax);
+        }
+        sg::scatter_cplx8(B20, B21, a.KC2, a.K * np, np, (blk - 1) * np + x, yrow, im, v,
+                          a.b2_bytes - (size_t)b * a.NT * a.KC2 * kPiece, a.status);
+      }
+    }
+  } else {
+    // ---- f = Z + X terms + M term and the RK4 stage update, runs of 8 rows
+    const int nlo = lane & 7, glo = lane >> 3;
+#pragma unroll 1
+    for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
+      const int jl = (wi >> 2) * 8 + nlo;
+      const int dl = ((wi & 3) * 4 + glo) * 8;
+      const int y = mt * kBM + dl, jj = nt * kBN + jl;
+      if (y < np) {
+        float f[8];
+        park8(jl, dl, f);
+        assemble_f(a, b, jj, y, f);
+        update8(a, b, jj, y, f, bad, range);
+      }
+    }
+  }
+  if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// Tile `local` of a GEMM 1 (kZ = false) or GEMM 2 launch over a.batch
+// instances: its operands and position.
+template <bool kZ>
+__device__ __forceinline__ void gemm_tile_of(const Args& a, int local, sg::Tile& T, int& b, int& mt, int& nt) {
   const int MT = kZ ? a.MT2 : a.MT1;
   const int KC = kZ ? a.KC2 : a.KC1;
-  const int b = blockIdx.x / (MT * a.NT);
-  const int tile = blockIdx.x % (MT * a.NT);
-  const int mt = tile / a.NT, nt = tile % a.NT;
+  b = local / (MT * a.NT);
+  const int tile = local % (MT * a.NT);
+  mt = tile / a.NT;
+  nt = tile % a.NT;
   const int g = a.G == 1 ? 0 : b % a.P;
-  sg::setup(S);
-  sg::Tile T;
   const size_t aoff = ((size_t)g * MT + mt) * KC * kPiece;
   const size_t boff = ((size_t)b * a.NT + nt) * KC * kPiece;
   for (int i = 0; i < 3; ++i) T.A[i] = (kZ ? a.A2[i] : a.A1[i]) + aoff;
@@ -176,72 +246,92 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
   T.a_avail = (kZ ? a.a2_bytes : a.a1_bytes) - aoff;
   T.b_avail = (kZ ? a.b2_bytes : a.b1_bytes) - boff;
   T.status = a.status;
+}
+
+// kZ = false: GEMM 1 (X and Y_k rows); kZ = true: GEMM 2 and the stage update.
+// One tile per CTA.
+template <bool kZ>
+__global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(Args a) {
+  extern __shared__ uint8_t smem_raw[];
+  sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  sg::setup(S);
+  sg::Tile T;
+  int b, mt, nt;
+  gemm_tile_of<kZ>(a, blockIdx.x, T, b, mt, nt);
   const float* ft = S.tile();
   if (sg::mainloop(S, T) && !*(volatile int*)&S.abort) {
-    const int u = t - sg::kEpiFirst, ew = u >> 5;
-    const int np = a.np;
-    bool bad = false, range = false;
-    if (!kZ) {
-      // ---- X rows (block 0): the tile columns into Xg, runs of 8 rows
-      const int nlo = lane & 7, glo = lane >> 3;
-#pragma unroll 1
-      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
-        const int jl = (wi >> 2) * 8 + nlo;
-        const int dl = ((wi & 3) * 4 + glo) * 8;
-        const int R = mt * kBM + dl;
-        const size_t xo = (size_t)b * inst_floats(a) + (size_t)(nt * kBN + jl) * np + R;
-        if (R < np && in_bounds(xo * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status)) {
-          float v[8];
-          sg::ld8(ft + jl * kFStride + dl, v);
-          sg::st8(a.Xg + xo, v);
-        }
-      }
-      // ---- Y_k rows (blocks 1..K): Y^dag into B2, runs of 8 columns of one row
-      const int r = u & 127, o0 = u >> 7;
-      constexpr int kGroups = sg::kEpiThreads / 128;
-      const int R = mt * kBM + r;
-      const int blk = R / np, yrow = R - blk * np;
-      if (blk >= 1 && blk <= a.K) {
-        uint8_t* B20 = a.B2[0] + (size_t)b * a.NT * a.KC2 * kPiece;
-        uint8_t* B21 = a.B2[1] + (size_t)b * a.NT * a.KC2 * kPiece;
-#pragma unroll 1
-        for (int i = 0; i < 16 / kGroups; ++i) {
-          const int cl = 8 * (o0 + kGroups * i);
-          const int jj = nt * kBN + cl;
-          const bool im = jj >= np;
-          const int x = im ? jj - np : jj;
-          float v[8];
-#pragma unroll
-          for (int e = 0; e < 8; ++e) {
-            // S2[(k-1) np + x][yrow] = conj(Y_k[yrow][x]): real part Yr, imaginary part -Yi
-            const float y = ft[(cl + e) * kFStride + r];
-            v[e] = __fmul_rn(im ? -y : y, a.sy);
-            range |= !(fabsf(v[e]) <= sg::kBMax);
-          }
-          sg::scatter_cplx8(B20, B21, a.KC2, a.K * np, np, (blk - 1) * np + x, yrow, im, v,
-                            a.b2_bytes - (size_t)b * a.NT * a.KC2 * kPiece, a.status);
-        }
-      }
-    } else {
-      // ---- f = Z + X terms + M term and the RK4 stage update, runs of 8 rows
-      const int nlo = lane & 7, glo = lane >> 3;
-#pragma unroll 1
-      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
-        const int jl = (wi >> 2) * 8 + nlo;
-        const int dl = ((wi & 3) * 4 + glo) * 8;
-        const int y = mt * kBM + dl, jj = nt * kBN + jl;
-        if (y < np) {
-          float f[8];
-          sg::ld8(ft + jl * kFStride + dl, f);
-          assemble_f(a, b, jj, y, f);
-          update8(a, b, jj, y, f, bad, range);
-        }
-      }
-    }
-    if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
-    if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+    fused_epilogue<kZ>(
+        a, b, mt, nt, [&](int c, int r) { return ft[c * kFStride + r]; },
+        [&](int c, int r, float (&v)[8]) { sg::ld8(ft + c * kFStride + r, v); });
   }
   sg::teardown(S, a.status);
+}
+
+// The GEMM 1 or GEMM 2 tiles of several instance groups (different
+// dimensions and operator counts) in one persistent launch: CTA j runs
+// tiles j, j + gridDim.x, ... of the concatenated tile list, whose groups
+// the host orders by decreasing chunks per tile (largest tiles first).
+constexpr int kMaxGroups = 16;
+struct Groups {
+  int n_groups, n_items;
+  int start[kMaxGroups + 1];          // first tile of each group in the list
+  Args g[kMaxGroups];
+};
+static_assert(sizeof(Groups) <= 30000, "kernel parameter space");
+
+template <bool kZ>
+__global__ void __launch_bounds__(sg::kThreads, 1) gemm_groups_kernel(const __grid_constant__ Groups m) {
+  extern __shared__ uint8_t smem_raw[];
+  sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  sg::setup(S);
+  sg::Seq q;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  auto group_of = [&](int item) {
+    int gi = 0;
+    while (gi + 1 < m.n_groups && item >= m.start[gi + 1]) ++gi;
+    return gi;
+  };
+  if (warp < 2) {
+    if (lane == 0) {
+      bool alive = true;
+      for (int item = blockIdx.x; item < m.n_items && alive; item += gridDim.x) {
+        const int gi = group_of(item);
+        sg::Tile T;
+        int b, mt, nt;
+        gemm_tile_of<kZ>(m.g[gi], item - m.start[gi], T, b, mt, nt);
+        alive = warp == 0 ? sg::seq_produce(S, T, q) : sg::seq_mma(S, T, q);
+      }
+      if (warp == 0)
+        sg::seq_produce_end(S, q, m.g[0].max_wait);
+      else
+        sg::seq_mma_end(S, m.g[0].max_wait);
+    }
+  } else {
+    const float* ft = S.lo;
+    for (int item = blockIdx.x; item < m.n_items; item += gridDim.x) {
+      const int gi = group_of(item);
+      sg::Tile T;
+      int b, mt, nt;
+      gemm_tile_of<kZ>(m.g[gi], item - m.start[gi], T, b, mt, nt);
+      const bool ok = sg::seq_drain(S, T, q);
+      const bool stop = sg::epi_bar_or(!ok || *(volatile int*)&S.abort);
+      if (!stop) {
+        fused_epilogue<kZ>(
+            m.g[gi], b, mt, nt, [&](int c, int r) { return ft[sg::park_idx(c, r)]; },
+            [&](int c, int r, float (&v)[8]) { sg::ld8_park(ft, c, r, v); });
+      }
+      sg::epi_bar();   // the parked tile is read before the next drain clears it
+      if (stop) break;
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (t == 0 && S.abort)
+    for (int i = 0; i < m.n_groups; ++i) atomicOr(m.g[i].status, LIME_FLAG_TIMEOUT);
+  if (warp == 0) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(S.tmem_base, sg::kTmemCols);
+  }
 }
 
 // 32 x 32 tiles of the state for the elementwise stage kernels: the
@@ -724,7 +814,22 @@ extern "C" size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32
   return lsm_layout(n, batch, n_generators, n_ops).total + (size_t)n_generators * n * n * 16;
 }
 
-extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream) {
+namespace {
+
+// The buffers of one streaming propagation inside its workspace.
+struct LsmRun {
+  lsm::Args a;
+  lsm::ConvertOut co;
+  LsmLayout L;
+  uint8_t* B1[2][2];
+  float* Sbuf[2];
+  double2* heff_t;
+  int B, K, G;
+};
+
+// Validates d, lays out its workspace, converts the operands and loads the
+// initial state (two launches on st).
+int lsm_prepare(const LimeLindbladStreamDesc* d, LsmRun& r, cudaStream_t st, int64_t& launches) {
   if (!d || d->n <= 0 || d->batch <= 0 || d->n_ops < 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
   if (!d->rho || !d->heff || !d->workspace || !d->status) return LIME_ERR_ARG;
   if (d->n_ops > 0 && !d->l_ops) return LIME_ERR_ARG;
@@ -744,25 +849,27 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   const size_t drive_bytes = d->n_drive > 0 ? (size_t)G * d->n * d->n * sizeof(double2) : 0;
   if (d->workspace_bytes < L.total + drive_bytes) return LIME_ERR_WORKSPACE;
   if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
-  const int B = d->batch;
-  cudaStream_t st = (cudaStream_t)stream;
+  r.L = L;
+  r.B = d->batch;
+  r.K = K;
+  r.G = G;
 
   uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
-  lsm::Args a{};
-  lsm::ConvertOut co{};
+  lsm::Args& a = r.a;
+  lsm::ConvertOut& co = r.co;
+  a = lsm::Args{};
+  co = lsm::ConvertOut{};
   a.n = d->n; a.np = L.np; a.W = L.W; a.NT = L.NT; a.K = K; a.P = P; a.G = G;
   a.KC1 = L.KC1; a.KC2 = L.KC2; a.MT1 = L.MT1; a.MT2 = L.MT2;
   for (int i = 0; i < 3; ++i) { a.A1[i] = co.A1[i] = w; w += L.a1; }
   for (int i = 0; i < 3; ++i) { a.A2[i] = co.A2[i] = w; w += L.a2; }
   a.rinv1 = co.rinv1 = reinterpret_cast<float*>(w); w += L.r1;
   a.rinv2 = co.rinv2 = reinterpret_cast<float*>(w); w += L.r2;
-  uint8_t* B1[2][2];
   for (int bb = 0; bb < 2; ++bb)
-    for (int i = 0; i < 2; ++i) { B1[bb][i] = w; w += L.b1; }
+    for (int i = 0; i < 2; ++i) { r.B1[bb][i] = w; w += L.b1; }
   for (int i = 0; i < 2; ++i) { a.B2[i] = w; w += L.b2; }
   a.Xg = reinterpret_cast<float*>(w); w += L.st;
-  float* Sbuf[2];
-  for (int i = 0; i < 2; ++i) { Sbuf[i] = reinterpret_cast<float*>(w); w += L.st; }
+  for (int i = 0; i < 2; ++i) { r.Sbuf[i] = reinterpret_cast<float*>(w); w += L.st; }
   a.Phi = reinterpret_cast<float*>(w); w += L.st;
   a.Plo = reinterpret_cast<float*>(w); w += L.st;
   a.Acc = reinterpret_cast<float*>(w); w += L.st;
@@ -784,29 +891,70 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
   a.max_wait = 1u << 26;
   a.a1_bytes = L.a1; a.a2_bytes = L.a2; a.b1_bytes = L.b1; a.b2_bytes = L.b2;
   a.st_floats = L.st / sizeof(float);
-  int64_t launches = 0;
+  r.heff_t = reinterpret_cast<double2*>(reinterpret_cast<uint8_t*>(d->workspace) + L.total);
 
   const int per_g = L.MT1 * 128 + (K > 0 ? L.MT2 * 128 : 0);
   lsm::convert_kernel<<<G * per_g, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride,
                                                   reinterpret_cast<const double2*>(d->l_ops), d->l_stride, a, co, 0);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
-  a.B1n[0] = B1[0][0]; a.B1n[1] = B1[0][1];
-  a.Sn = Sbuf[0];
-  const size_t runs = (size_t)B * L.W * (L.np / 8);
+  a.B1n[0] = r.B1[0][0]; a.B1n[1] = r.B1[0][1];
+  a.Sn = r.Sbuf[0];
+  const size_t runs = (size_t)r.B * L.W * (L.np / 8);
   const int eb = (int)((runs + 255) / 256 < 65535 ? (runs + 255) / 256 : 65535);
-  const int tb = B * (L.np / 32) * (L.np / 32);            // 32 x 32 state tiles
-  lsm::init_kernel<<<eb, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->rho), B);
+  lsm::init_kernel<<<eb, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->rho), r.B);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
+  return LIME_OK;
+}
 
+// stage s with stage-input buffers cur (read) and cur ^ 1 (written)
+void lsm_bind_stage(LsmRun& r, int s, int cur) {
+  r.a.rk.stage = s;
+  r.a.B1c[0] = r.B1[cur][0]; r.a.B1c[1] = r.B1[cur][1];
+  r.a.B1n[0] = r.B1[cur ^ 1][0]; r.a.B1n[1] = r.B1[cur ^ 1][1];
+  r.a.Sc = r.Sbuf[cur];
+  r.a.Sn = r.Sbuf[cur ^ 1];
+}
+
+int lsm_observe(const LimeLindbladStreamDesc* d, LsmRun& r, int step, cudaStream_t st, int64_t& launches) {
+  const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  if (d->n_obs > 0 && ((step + 1) % obs_every) == 0) {
+    lsm::observe_kernel<<<r.B * d->n_obs, 128, 0, st>>>(r.a, reinterpret_cast<const double2*>(d->obs_ops),
+                                                        d->obs_stride, d->n_obs,
+                                                        reinterpret_cast<double2*>(d->obs_out),
+                                                        d->n_steps / obs_every, (step + 1) / obs_every - 1);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+  }
+  return LIME_OK;
+}
+
+int lsm_final(const LimeLindbladStreamDesc* d, LsmRun& r, cudaStream_t st, int64_t& launches) {
+  const size_t tot = (size_t)r.B * d->n * d->n;
+  const int fb = (int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535);
+  lsm::final_kernel<<<fb, 256, 0, st>>>(r.a, reinterpret_cast<double2*>(d->rho), r.B);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  return LIME_OK;
+}
+
+}  // namespace
+
+extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  int64_t launches = 0;
+  LsmRun r;
+  const int rc = lsm_prepare(d, r, st, launches);
+  if (rc != LIME_OK) return rc;
+  const LsmLayout& L = r.L;
+  const int B = r.B, K = r.K, G = r.G;
+  lsm::Args& a = r.a;
+  const int tb = B * (L.np / 32) * (L.np / 32);            // 32 x 32 state tiles
   const size_t smem = sg::kSmemBytes;
   LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
-  const int n_slots = d->n_steps / obs_every;
   int cur = 0;
-  double2* heff_t = reinterpret_cast<double2*>(reinterpret_cast<uint8_t*>(d->workspace) + L.total);
   for (int step = 0; step < d->n_steps; ++step) {
     if (d->n_drive > 0) {
       // Heff(t) of this step, re-split into the GEMM 1 pieces
@@ -814,19 +962,15 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
       const int hb = (int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535);
       lsm::heff_t_kernel<<<hb, 256, 0, st>>>(reinterpret_cast<const double2*>(d->heff), d->heff_stride, G, d->n,
                                              reinterpret_cast<const double2*>(d->drive_ops),
-                                             d->drive_coef + (size_t)step * d->n_drive, d->n_drive, heff_t);
+                                             d->drive_coef + (size_t)step * d->n_drive, d->n_drive, r.heff_t);
       LIME_CUDA_TRY(cudaGetLastError());
-      lsm::convert_kernel<<<G * L.np, 256, 0, st>>>(heff_t, G == 1 ? 0 : (int64_t)d->n * d->n, nullptr, 0, a,
-                                                    co, 1);
+      lsm::convert_kernel<<<G * L.np, 256, 0, st>>>(r.heff_t, G == 1 ? 0 : (int64_t)d->n * d->n, nullptr, 0, a,
+                                                    r.co, 1);
       LIME_CUDA_TRY(cudaGetLastError());
       launches += 2;
     }
     for (int s = 0; s < 4; ++s) {
-      a.rk.stage = s;
-      a.B1c[0] = B1[cur][0]; a.B1c[1] = B1[cur][1];
-      a.B1n[0] = B1[cur ^ 1][0]; a.B1n[1] = B1[cur ^ 1][1];
-      a.Sc = Sbuf[cur];
-      a.Sn = Sbuf[cur ^ 1];
+      lsm_bind_stage(r, s, cur);
       lsm::gemm_kernel<false><<<B * L.MT1 * L.NT, sg::kThreads, smem, st>>>(a);
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
@@ -839,24 +983,112 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
       ++launches;
       cur ^= 1;
     }
-    if (d->n_obs > 0 && ((step + 1) % obs_every) == 0) {
-      lsm::observe_kernel<<<B * d->n_obs, 128, 0, st>>>(a, reinterpret_cast<const double2*>(d->obs_ops),
-                                                        d->obs_stride, d->n_obs,
-                                                        reinterpret_cast<double2*>(d->obs_out), n_slots,
-                                                        (step + 1) / obs_every - 1);
-      LIME_CUDA_TRY(cudaGetLastError());
-      ++launches;
-    }
+    const int orc = lsm_observe(d, r, step, st, launches);
+    if (orc != LIME_OK) return orc;
   }
-  const size_t tot = (size_t)B * d->n * d->n;
-  const int fb = (int)((tot + 255) / 256 < 65535 ? (tot + 255) / 256 : 65535);
-  lsm::final_kernel<<<fb, 256, 0, st>>>(a, reinterpret_cast<double2*>(d->rho), B);
-  LIME_CUDA_TRY(cudaGetLastError());
-  ++launches;
+  const int frc = lsm_final(d, r, st, launches);
+  if (frc != LIME_OK) return frc;
   count_launch(launches);
   return LIME_OK;
 }
 
+extern "C" int32_t lime_lindblad_stream_max_groups(void) { return lsm::kMaxGroups; }
+
+extern "C" int lime_lindblad_rk4_stream_groups(const LimeLindbladStreamDesc* descs, int32_t n_groups,
+                                               int32_t n_ctas, int32_t order, void* stream) {
+  if (!descs || n_groups <= 0 || n_ctas < 0 || order < 0 || order > 1) return LIME_ERR_ARG;
+  if (n_groups > lsm::kMaxGroups) return LIME_ERR_UNSUPPORTED;
+  for (int i = 0; i < n_groups; ++i) {
+    const LimeLindbladStreamDesc& d = descs[i];
+    if (d.n_drive != 0) return LIME_ERR_UNSUPPORTED;
+    if (d.n_steps != descs[0].n_steps || d.dt != descs[0].dt ||
+        (d.obs_every > 0 ? d.obs_every : 1) != (descs[0].obs_every > 0 ? descs[0].obs_every : 1))
+      return LIME_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int64_t launches = 0;
+  LsmRun runs[lsm::kMaxGroups];
+  for (int i = 0; i < n_groups; ++i) {
+    const int rc = lsm_prepare(&descs[i], runs[i], st, launches);
+    if (rc != LIME_OK) return rc;
+  }
+  int dev = 0, sms = 0;
+  LIME_CUDA_TRY(cudaGetDevice(&dev));
+  LIME_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const size_t smem = sg::kSmemBytes;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_groups_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(lsm::gemm_groups_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+  // tile lists: groups by decreasing chunks per tile (order 1), or as given (order 0)
+  int ord1[lsm::kMaxGroups], ord2[lsm::kMaxGroups];
+  int n2 = 0;
+  for (int i = 0; i < n_groups; ++i) {
+    ord1[i] = i;
+    if (runs[i].K > 0) ord2[n2++] = i;
+  }
+  if (order == 1) {
+    auto sort_by = [&](int* o, int cnt, bool z) {
+      for (int i = 1; i < cnt; ++i)
+        for (int j = i; j > 0; --j) {
+          const int kj = z ? runs[o[j]].L.KC2 : runs[o[j]].L.KC1;
+          const int kp = z ? runs[o[j - 1]].L.KC2 : runs[o[j - 1]].L.KC1;
+          if (kj > kp) { const int tmp = o[j]; o[j] = o[j - 1]; o[j - 1] = tmp; } else break;
+        }
+    };
+    sort_by(ord1, n_groups, false);
+    sort_by(ord2, n2, true);
+  }
+  auto fill = [&](lsm::Groups& m, const int* o, int cnt, bool z) {
+    m.n_groups = cnt;
+    m.start[0] = 0;
+    for (int i = 0; i < cnt; ++i) {
+      const LsmRun& r = runs[o[i]];
+      m.g[i] = r.a;
+      m.start[i + 1] = m.start[i] + r.B * (z ? r.L.MT2 : r.L.MT1) * r.L.NT;
+    }
+    m.n_items = m.start[cnt];
+  };
+  auto grid_of = [&](int items) {
+    const int g = n_ctas > 0 ? n_ctas : sms;
+    return g < items ? g : items;
+  };
+  lsm::Groups m1, m2;   // launch parameters (copied at each launch)
+  int cur = 0;
+  for (int step = 0; step < descs[0].n_steps; ++step) {
+    for (int s = 0; s < 4; ++s) {
+      for (int i = 0; i < n_groups; ++i) lsm_bind_stage(runs[i], s, cur);
+      fill(m1, ord1, n_groups, false);
+      lsm::gemm_groups_kernel<false><<<grid_of(m1.n_items), sg::kThreads, smem, st>>>(m1);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+      if (n2 > 0) {
+        fill(m2, ord2, n2, true);
+        lsm::gemm_groups_kernel<true><<<grid_of(m2.n_items), sg::kThreads, smem, st>>>(m2);
+        LIME_CUDA_TRY(cudaGetLastError());
+        ++launches;
+      }
+      for (int i = 0; i < n_groups; ++i) {
+        if (runs[i].K > 0) continue;
+        const int tb = runs[i].B * (runs[i].L.np / 32) * (runs[i].L.np / 32);
+        lsm::finish_kernel<<<tb, 256, 0, st>>>(runs[i].a);
+        LIME_CUDA_TRY(cudaGetLastError());
+        ++launches;
+      }
+      cur ^= 1;
+    }
+    for (int i = 0; i < n_groups; ++i) {
+      const int orc = lsm_observe(&descs[i], runs[i], step, st, launches);
+      if (orc != LIME_OK) return orc;
+    }
+  }
+  for (int i = 0; i < n_groups; ++i) {
+    const int frc = lsm_final(&descs[i], runs[i], st, launches);
+    if (frc != LIME_OK) return frc;
+  }
+  count_launch(launches);
+  return LIME_OK;
+}
 
 extern "C" size_t lime_lindblad_adjoint_stream_workspace(int32_t n, int32_t batch, int32_t n_generators,
                                                          int32_t seg_steps) {

@@ -63,6 +63,19 @@ struct StageArgs {
   float* Ghi = nullptr;
   float* Glo = nullptr;
   const float* col_inv = nullptr;
+  // modes 4 and 5 (the 3M complex product, lime_redfield_rk4_split3): per
+  // real product p = 0, 1, 2 (Lr Sr, Li Si, (Lr + Li)(Sr + Si); for the
+  // observables Etr, Eti, Etr + Eti) its A pieces, row scales, current B
+  // pieces and inverse B scale; mode 4 writes the products' two-sum words
+  // ([Rq][Dp] each), mode 5 adds product p to the observables with the
+  // coefficients obs_c3[p] = (to Re, to Im)
+  const uint8_t* A3[3][3] = {};
+  const float* rinv3[3] = {};
+  const uint8_t* B3c[3][2] = {};
+  float inv_sb3[3] = {};
+  float* Thi3[3] = {};
+  float* Tlo3[3] = {};
+  float obs_c3[3][2] = {};
 };
 
 // kMode 0: one RK4 stage, Y = L S over the full K, fused stage update.
@@ -71,17 +84,25 @@ struct StageArgs {
 // yb = L^dag a (A = the L^dag pieces, B = a), fused adjoint combination.
 // kMode 3: the generator gradient sum_i a_i y_i^dag of one step (A = the
 // adjoint stage inputs, B = the stage inputs), added to the accumulator.
+// kMode 4: the three real products of the 3M form of one stage (product p
+// = blockIdx.x / (MT NT)), two-sum words stored for stage3_kernel.  kMode 5:
+// the observables of the 3M state, K split over KS CTAs per product.
 template <int kMode>
 __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
-  constexpr bool kObserve = kMode == 1;
+  constexpr bool kObserve = kMode == 1 || kMode == 5;
+  constexpr bool k3m = kMode == 4 || kMode == 5;
   extern __shared__ uint8_t smem_raw[];
   sg::Smem& S = *reinterpret_cast<sg::Smem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int t = threadIdx.x, lane = t & 31;
-  const int tile = kObserve ? (int)(blockIdx.x % (a.MT * a.NT)) : (int)blockIdx.x;
+  const int tiles = a.MT * a.NT;
+  const int per_p = kObserve ? tiles * a.KS : tiles;
+  const int p = k3m ? (int)(blockIdx.x / per_p) : 0;
+  const int rem = (int)(blockIdx.x % per_p);
+  const int tile = rem % tiles;
   const int mt = tile / a.NT, nt = tile % a.NT;
   int c0 = 0, KC = a.KC;                      // this CTA's chunk range [c0, c0 + KC)
   if (kObserve) {
-    const int ks = blockIdx.x / (a.MT * a.NT);
+    const int ks = rem / tiles;
     const int g0 = ks * a.groups_per_split;
     const int g1 = min(g0 + a.groups_per_split, a.KC / kGroup);
     c0 = kGroup * g0;
@@ -89,12 +110,13 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
   }
   sg::setup(S);
   sg::Tile T;
-  for (int i = 0; i < 3; ++i) T.A[i] = a.A[i] + (size_t)mt * a.KC * kPiece;
-  for (int i = 0; i < 2; ++i) T.B[i] = a.Bc[i] + (size_t)nt * a.KC * kPiece;
+  for (int i = 0; i < 3; ++i) T.A[i] = (k3m ? a.A3[p][i] : a.A[i]) + (size_t)mt * a.KC * kPiece;
+  for (int i = 0; i < 2; ++i) T.B[i] = (k3m ? a.B3c[p][i] : a.Bc[i]) + (size_t)nt * a.KC * kPiece;
   T.c0 = c0;
   T.n_chunks = KC;
-  T.row_inv = a.row_inv + (size_t)mt * kBM;
-  T.inv_sb = (kMode == 2) ? ldexpf(1.f, -*a.sl_exp) : a.inv_sb;
+  T.row_inv = (k3m ? a.rinv3[p] : a.row_inv) + (size_t)mt * kBM;
+  T.inv_sb = (kMode == 2) ? ldexpf(1.f, -*a.sl_exp) : (k3m ? a.inv_sb3[p] : a.inv_sb);
+  T.park_split = kMode == 4;
   T.max_wait = a.max_wait;
   T.a_avail = a.a_bytes - (size_t)mt * a.KC * kPiece;
   T.b_avail = a.b_bytes - (size_t)nt * a.KC * kPiece;
@@ -110,11 +132,34 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
 #pragma unroll 4
         for (int c = 0; c < sg::kEpiCols; ++c) {
           const int jj = nt * kBN + sg::kEpiCols * hh + c;
-          const int j = jj < a.Rp ? jj : jj - a.Rp;
-          if (j < a.R)
-            atomicAdd(a.obs + 2 * ((size_t)j * a.n_obs + o) + (jj < a.Rp ? 0 : 1),
-                      (double)ft[(sg::kEpiCols * hh + c) * kFStride + r]);
+          const double v = (double)ft[(sg::kEpiCols * hh + c) * kFStride + r];
+          if (k3m) {
+            // real product p: column jj is right-hand side jj
+            if (jj < a.R) {
+              double* ob = a.obs + 2 * ((size_t)jj * a.n_obs + o);
+              if (a.obs_c3[p][0] != 0.f) atomicAdd(ob, (double)a.obs_c3[p][0] * v);
+              if (a.obs_c3[p][1] != 0.f) atomicAdd(ob + 1, (double)a.obs_c3[p][1] * v);
+            }
+          } else {
+            const int j = jj < a.Rp ? jj : jj - a.Rp;
+            if (j < a.R) atomicAdd(a.obs + 2 * ((size_t)j * a.n_obs + o) + (jj < a.Rp ? 0 : 1), v);
+          }
         }
+      }
+    } else if (kMode == 4) {
+      // ---- 3M product p: its two-sum words (hi parked in the ring, lo in S.lo), runs of 8 rows
+      const int nlo = lane & 7, glo = lane >> 3;
+#pragma unroll 1
+      for (int wi = ew; wi < 64; wi += sg::kEpiWarps) {
+        const int jl = (wi >> 2) * 8 + nlo;
+        const int dl = ((wi & 3) * 4 + glo) * 8;
+        const size_t e = (size_t)(nt * kBN + jl) * a.Dp + mt * kBM + dl;
+        if (!in_bounds(e * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status)) continue;
+        float h[8], l[8];
+        sg::ld8(ft + jl * kFStride + dl, h);
+        sg::ld8(S.lo + jl * kBM + dl, l);
+        sg::st8(a.Thi3[p] + e, h);
+        sg::st8(a.Tlo3[p] + e, l);
       }
     } else if (kMode == 2) {
       // ---- adjoint stage: yb = L^dag a_i in runs of 8 rows; a_{i-1} or the new lam
@@ -303,48 +348,66 @@ __global__ void adj_lam_out_kernel(const float* Lhi, const float* Llo, int D, in
 }
 
 // lam += Et^dag g (the observables recorded after the step, g [R][n_obs]
-// complex128, or none) and max |lam| of the step.  One thread per row d and
-// a chunk of 8 right-hand sides: Et[o][d] is read once per chunk
-// (coalesced across the warp's rows) and the chunk's g from shared memory.
-__global__ void adj_src_kernel(float* Lhi, float* Llo, int D, int R, int Dp, int Rp, const float2* EtF, int n_obs,
-                               const double2* g, unsigned* lmax) {
-  extern __shared__ float2 gs[];   // [8][n_obs]
-  const int chunks = Rp / 8;
-  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+// complex128, or none) and max |lam| of the step.  A CTA owns a 64-row x
+// 32-column tile of lam (4 x 2 entries a thread) and runs over the
+// observables in chunks of 16 staged in shared memory; each entry sums its
+// observables in increasing order.
+constexpr int kSrcTD = 64, kSrcTR = 32, kSrcKO = 16;
+__global__ void __launch_bounds__(256) adj_src_kernel(float* Lhi, float* Llo, int D, int R, int Dp, int Rp,
+                                                      const float2* EtF, int n_obs, const double2* g, unsigned* lmax) {
+  __shared__ float2 es[kSrcKO][kSrcTD];
+  __shared__ float2 gs[kSrcTR][kSrcKO + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int d0 = blockIdx.x * kSrcTD, r0 = blockIdx.y * kSrcTR;
+  float sr[2][4], si[2][4];
+#pragma unroll
+  for (int v = 0; v < 2; ++v)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) sr[v][u] = si[v][u] = 0.f;
+  if (g != nullptr) {
+    for (int o0 = 0; o0 < n_obs; o0 += kSrcKO) {
+      __syncthreads();
+      for (int q = threadIdx.x; q < kSrcKO * kSrcTD; q += blockDim.x) {
+        const int o = o0 + q / kSrcTD, dd = d0 + q % kSrcTD;
+        es[q / kSrcTD][q % kSrcTD] = (o < n_obs && dd < D) ? EtF[(size_t)o * D + dd] : make_float2(0.f, 0.f);
+      }
+      for (int q = threadIdx.x; q < kSrcTR * kSrcKO; q += blockDim.x) {
+        const int rr = r0 + q / kSrcKO, o = o0 + q % kSrcKO;
+        const double2 v = (rr < R && o < n_obs) ? g[(size_t)rr * n_obs + o] : make_double2(0.0, 0.0);
+        gs[q / kSrcKO][q % kSrcKO] = make_float2((float)v.x, (float)v.y);
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < kSrcKO; ++k) {
+        float2 e[4], gv[2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) e[u] = es[k][tx + 16 * u];
+#pragma unroll
+        for (int v = 0; v < 2; ++v) gv[v] = gs[ty + 16 * v][k];
+#pragma unroll
+        for (int v = 0; v < 2; ++v)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            // conj(Et) g = (er gr + ei gi) + i (er gi - ei gr)
+            sr[v][u] = __fmaf_rn(e[u].x, gv[v].x, __fmaf_rn(e[u].y, gv[v].y, sr[v][u]));
+            si[v][u] = __fmaf_rn(e[u].x, gv[v].y, __fmaf_rn(-e[u].y, gv[v].x, si[v][u]));
+          }
+      }
+    }
+  }
   float mx = 0.f;
-  for (int ch = blockIdx.y; ch < chunks; ch += gridDim.y) {
-    const int r0 = ch * 8;
-    if (g != nullptr) {
-      __syncthreads();
-      for (int q = threadIdx.x; q < 8 * n_obs; q += blockDim.x) {
-        const int rr = r0 + q / n_obs, o = q % n_obs;
-        const double2 v = rr < R ? g[(size_t)rr * n_obs + o] : make_double2(0.0, 0.0);
-        gs[q] = make_float2((float)v.x, (float)v.y);
-      }
-      __syncthreads();
-    }
-    if (d >= Dp) continue;
-    float sr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, si[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (g != nullptr && d < D) {
-      for (int o = 0; o < n_obs; ++o) {
-        const float2 et = EtF[(size_t)o * D + d];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          // conj(Et) g = (er gr + ei gi) + i (er gi - ei gr)
-          const float2 gv = gs[i * n_obs + o];
-          sr[i] = __fmaf_rn(et.x, gv.x, __fmaf_rn(et.y, gv.y, sr[i]));
-          si[i] = __fmaf_rn(et.x, gv.y, __fmaf_rn(-et.y, gv.x, si[i]));
-        }
-      }
-    }
+  for (int v = 0; v < 2; ++v)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const size_t er = (size_t)(r0 + i) * Dp + d, ei = (size_t)(Rp + r0 + i) * Dp + d;
+    for (int u = 0; u < 4; ++u) {
+      const int d = d0 + tx + 16 * u, r = r0 + ty + 16 * v;
+      if (d >= Dp || r >= Rp) continue;
+      const size_t er = (size_t)r * Dp + d, ei = (size_t)(Rp + r) * Dp + d;
       float hr = Lhi[er], hi = Lhi[ei];
-      if (g != nullptr && d < D && r0 + i < R) {
+      if (g != nullptr && d < D && r < R) {
         float lr = Llo[er], li = Llo[ei];
-        hr = rk4_final_f32(hr, 0.f, sr[i], 1.f, 0.f, lr);
-        hi = rk4_final_f32(hi, 0.f, si[i], 1.f, 0.f, li);
+        hr = rk4_final_f32(hr, 0.f, sr[v][u], 1.f, 0.f, lr);
+        hi = rk4_final_f32(hi, 0.f, si[v][u], 1.f, 0.f, li);
         Lhi[er] = hr;
         Llo[er] = lr;
         Lhi[ei] = hi;
@@ -352,7 +415,6 @@ __global__ void adj_src_kernel(float* Lhi, float* Llo, int D, int R, int Dp, int
       }
       mx = fmaxf(mx, fmaxf(fabsf(hr), fabsf(hi)));
     }
-  }
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0 && mx > 0.f) atomicMax(lmax, __float_as_uint(mx));
 }
@@ -395,50 +457,64 @@ __global__ void adj_start_kernel(StageArgs a, float dt6) {
 }
 
 // grad_E[o][b][a] += sum_r g[r][o] conj(rho[(a, b)][r]) for the observables
-// recorded after the step (rho planar [W][Dp] fp32).  One thread per row d
-// and a chunk of 8 observables: rho is read once per chunk (coalesced), g
-// for the chunk comes from shared memory.
-__global__ void adj_grad_obs_kernel(const float* rho, const double2* g, int n_obs, int n, int R, int Dp, int Rp,
-                                    double2* gE) {
-  constexpr int kRC = 256;          // right-hand sides per shared-memory chunk
-  __shared__ float2 gs[kRC * 8];   // [r][8]
+// recorded after the step (rho planar [W][Dp] fp32).  A CTA owns 32
+// observables x 64 rows (2 x 4 a thread) and runs over the right-hand sides
+// in chunks of 16 staged in shared memory; each entry sums them in
+// increasing order.
+constexpr int kGoTD = 64, kGoTO = 32, kGoKR = 16;
+__global__ void __launch_bounds__(256) adj_grad_obs_kernel(const float* rho, const double2* g, int n_obs, int n, int R,
+                                                           int Dp, int Rp, double2* gE) {
+  __shared__ float2 ps[kGoKR][kGoTD];
+  __shared__ float2 gs[kGoTO][kGoKR + 1];
   const int D = n * n;
-  const int d = blockIdx.x * blockDim.x + threadIdx.x;
-  for (int o0 = blockIdx.y * 8; o0 < n_obs; o0 += gridDim.y * 8) {
-    float vr[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vi[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int rc = 0; rc < R; rc += kRC) {
-      const int rn = R - rc < kRC ? R - rc : kRC;
-      __syncthreads();
-      for (int q = threadIdx.x; q < 8 * rn; q += blockDim.x) {
-        const int r = rc + q / 8, o = o0 + q % 8;
-        const double2 v = o < n_obs ? g[(size_t)r * n_obs + o] : make_double2(0.0, 0.0);
-        gs[q] = make_float2((float)v.x, (float)v.y);
-      }
-      __syncthreads();
-      if (d < D) {
-        for (int rr = 0; rr < rn; ++rr) {
-          const int r = rc + rr;
-          const float pr = rho[(size_t)r * Dp + d], pi = rho[(size_t)(Rp + r) * Dp + d];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int d0 = blockIdx.x * kGoTD, o0 = blockIdx.y * kGoTO;
+  float vr[2][4], vi[2][4];
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            // g conj(rho) = (gr pr + gi pi) + i (gi pr - gr pi)
-            const float2 gv = gs[rr * 8 + i];
-            vr[i] = __fmaf_rn(gv.x, pr, __fmaf_rn(gv.y, pi, vr[i]));
-            vi[i] = __fmaf_rn(gv.y, pr, __fmaf_rn(-gv.x, pi, vi[i]));
-          }
-        }
-      }
+  for (int v = 0; v < 2; ++v)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) vr[v][u] = vi[v][u] = 0.f;
+  for (int r0 = 0; r0 < R; r0 += kGoKR) {
+    __syncthreads();
+    for (int q = threadIdx.x; q < kGoKR * kGoTD; q += blockDim.x) {
+      const int r = r0 + q / kGoTD, d = d0 + q % kGoTD;
+      ps[q / kGoTD][q % kGoTD] = (r < R && d < D)
+                                     ? make_float2(rho[(size_t)r * Dp + d], rho[(size_t)(Rp + r) * Dp + d])
+                                     : make_float2(0.f, 0.f);
     }
-    if (d >= D) continue;
-    const int ia = d / n, ib = d % n;
+    for (int q = threadIdx.x; q < kGoTO * kGoKR; q += blockDim.x) {
+      const int o = o0 + q / kGoKR, r = r0 + q % kGoKR;
+      const double2 v = (o < n_obs && r < R) ? g[(size_t)r * n_obs + o] : make_double2(0.0, 0.0);
+      gs[q / kGoKR][q % kGoKR] = make_float2((float)v.x, (float)v.y);
+    }
+    __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      if (o0 + i < n_obs) {
-        double2& t = gE[(size_t)(o0 + i) * D + (size_t)ib * n + ia];
-        t = make_double2(t.x + (double)vr[i], t.y + (double)vi[i]);
-      }
+    for (int k = 0; k < kGoKR; ++k) {
+      float2 p[4], gv[2];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) p[u] = ps[k][tx + 16 * u];
+#pragma unroll
+      for (int v = 0; v < 2; ++v) gv[v] = gs[ty + 16 * v][k];
+#pragma unroll
+      for (int v = 0; v < 2; ++v)
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          // g conj(rho) = (gr pr + gi pi) + i (gi pr - gr pi)
+          vr[v][u] = __fmaf_rn(gv[v].x, p[u].x, __fmaf_rn(gv[v].y, p[u].y, vr[v][u]));
+          vi[v][u] = __fmaf_rn(gv[v].y, p[u].x, __fmaf_rn(-gv[v].x, p[u].y, vi[v][u]));
+        }
     }
   }
+#pragma unroll
+  for (int v = 0; v < 2; ++v)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int d = d0 + tx + 16 * u, o = o0 + ty + 16 * v;
+      if (d >= D || o >= n_obs) continue;
+      const int ia = d / n, ib = d % n;
+      double2& t = gE[(size_t)o * D + (size_t)ib * n + ia];
+      t = make_double2(t.x + (double)vr[v][u], t.y + (double)vi[v][u]);
+    }
 }
 
 // A pieces of the gradient GEMM: row d, K index kk = i Rp + r over the four
@@ -546,6 +622,127 @@ __global__ void final_state_kernel(const float* Phi, const float* Plo, int Dp, i
     const size_t er = (size_t)j * Dp + d, ei = (size_t)(j + Rp) * Dp + d;
     rho[e] = make_double2((double)Phi[er] + (double)Plo[er], (double)Phi[ei] + (double)Plo[ei]);
   }
+}
+
+// ---------------------------------------------------------------- the 3M form
+// (lime_redfield_rk4_split3)  Y = L S as three real products, T1 = Lr Sr,
+// T2 = Li Si, T3 = (Lr + Li)(Sr + Si): Yr = T1 - T2, Yi = T3 - T1 - T2 —
+// three quarters of the multiplications of the block form.  State [2Rq][Dp]
+// (columns j < Rq real parts, Rq + j imaginary parts), operands Sr, Si and
+// Sr + Si as separate real B operands ([Rq/128][Dp/64] pieces each).
+
+// A pieces of row `row` of a real part of L (transposed = 0) or of the
+// observables (transposed = 1, element (o, a n + b) = E_o[b][a]): comp 0 the
+// real part, 1 the imaginary part, 2 their sum (formed in FP64).
+__global__ void convert_real_rows_kernel(const double2* M, int transposed, int comp, int n, int rows, int D, int KC,
+                                         uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
+  const int row = blockIdx.x;
+  auto value = [&](int kk) -> double {
+    if (kk >= D) return 0.0;
+    double2 z;
+    if (transposed == 0) {
+      z = M[(size_t)row * D + kk];
+    } else {
+      const int ia = kk / n, ib = kk - ia * n;
+      z = M[(size_t)row * D + (size_t)ib * n + ia];
+    }
+    return comp == 0 ? z.x : (comp == 1 ? z.y : z.x + z.y);
+  };
+  sg::convert_row_values(value, row, row < rows, KC * sg::kCK, KC, A0, A1, A2, row_inv);
+}
+
+struct Stage3 {
+  uint8_t* Bn[3][2];       // next stage input: Sr, Si, Sr + Si (two pieces each)
+  const float* Thi[3];     // T1, T2, T3 two-sum words, [Rq][Dp]
+  const float* Tlo[3];
+  int Rq, KC3;
+  float sb_sum;            // scale of the sum operand
+  size_t b_bytes;          // bytes of one piece buffer
+};
+
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// the three B operands of 8 rows d..d+7 of right-hand side j
+__device__ __forceinline__ void store_b3(const StageArgs& a, const Stage3& g, int j, int d, const float (&xr)[8],
+                                         const float (&xi)[8], bool& range) {
+  float vr[8], vi[8], vs[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    vr[i] = __fmul_rn(xr[i], a.sb);
+    vi[i] = __fmul_rn(xi[i], a.sb);
+    vs[i] = __fmul_rn(__fadd_rn(xr[i], xi[i]), g.sb_sum);
+    range |= !(fabsf(vr[i]) <= sg::kBMax) || !(fabsf(vi[i]) <= sg::kBMax) || !(fabsf(vs[i]) <= sg::kBMax);
+  }
+  sg::store_b8(g.Bn[0][0], g.Bn[0][1], g.KC3, j, d, vr, false, g.b_bytes, a.status);
+  sg::store_b8(g.Bn[1][0], g.Bn[1][1], g.KC3, j, d, vi, false, g.b_bytes, a.status);
+  sg::store_b8(g.Bn[2][0], g.Bn[2][1], g.KC3, j, d, vs, false, g.b_bytes, a.status);
+}
+
+// state and the first three B operands from complex128 rho [R][D]; one
+// thread per run of 8 rows of one right-hand side
+__global__ void init_state3_kernel(StageArgs a, Stage3 g, const double2* rho, int D, int R) {
+  const size_t total = (size_t)g.Rq * (a.Dp / 8);
+  bool range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(q / (a.Dp / 8)), d = (int)(q % (a.Dp / 8)) * 8;
+    float hr[8], lr[8], hi[8], li[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      double2 z = make_double2(0.0, 0.0);
+      if (d + i < D && j < R) z = rho[(size_t)j * D + d + i];
+      hr[i] = (float)z.x;
+      lr[i] = (float)(z.x - (double)hr[i]);
+      hi[i] = (float)z.y;
+      li[i] = (float)(z.y - (double)hi[i]);
+    }
+    const size_t er = (size_t)j * a.Dp + d, ei = (size_t)(g.Rq + j) * a.Dp + d;
+    sg::st8(a.Phi + er, hr);
+    sg::st8(a.Plo + er, lr);
+    sg::st8(a.Phi + ei, hi);
+    sg::st8(a.Plo + ei, li);
+    store_b3(a, g, j, d, hr, hi, range);
+  }
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// Y from the three products (float-float differences, rounded once), the
+// RK4 stage update of both components and the next three B operands
+__global__ void stage3_kernel(StageArgs a, Stage3 g) {
+  const size_t total = (size_t)g.Rq * (a.Dp / 8);
+  const sg::RK4 k4{a.stage, a.c_half, a.c_full, a.c_sixth, a.c_sixth_lo};
+  bool bad = false, range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(q / (a.Dp / 8)), d = (int)(q % (a.Dp / 8)) * 8;
+    const size_t e = (size_t)j * a.Dp + d;
+    float h1[8], l1[8], h2[8], l2[8], h3[8], l3[8];
+    sg::ld8(g.Thi[0] + e, h1);
+    sg::ld8(g.Tlo[0] + e, l1);
+    sg::ld8(g.Thi[1] + e, h2);
+    sg::ld8(g.Tlo[1] + e, l2);
+    sg::ld8(g.Thi[2] + e, h3);
+    sg::ld8(g.Tlo[2] + e, l3);
+    float yr[8], yi[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      float s, er;
+      two_sum(h1[i], -h2[i], s, er);
+      yr[i] = __fadd_rn(s, __fadd_rn(er, __fsub_rn(l1[i], l2[i])));
+      float s1, e1, s2, e2;
+      two_sum(h3[i], -h1[i], s1, e1);
+      two_sum(s1, -h2[i], s2, e2);
+      yi[i] = __fadd_rn(s2, __fadd_rn(__fadd_rn(e1, e2), __fsub_rn(__fsub_rn(l3[i], l1[i]), l2[i])));
+    }
+    float svr[8], svi[8];
+    sg::rk4_stage8(k4, a.Phi, a.Plo, a.Acc, e, yr, svr, bad);
+    sg::rk4_stage8(k4, a.Phi, a.Plo, a.Acc, (size_t)(g.Rq + j) * a.Dp + d, yi, svi, bad);
+    store_b3(a, g, j, d, svr, svi, range);
+  }
+  if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
 }
 
 }  // namespace rsp
@@ -701,6 +898,205 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   }
   const int fb = (int)(((size_t)d->n_rhs * D + 255) / 256);
   rsp::final_state_kernel<<<fb < 65535 ? fb : 65535, 256, 0, st>>>(Phi, Plo, Dp, Rp,
+                                                                     reinterpret_cast<double2*>(d->rho), D, d->n_rhs);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  count_launch(launches);
+  return LIME_OK;
+}
+
+// ---------------------------------------------------------------- the 3M form
+namespace {
+
+struct Rs3Layout {
+  int D, Dp, Rq, KC3, MT, NT3, MTo;
+  size_t apiece, epiece, bpiece, tarr, state, rows;
+  size_t total;
+};
+
+Rs3Layout rs3_layout(int n, int R, int n_obs) {
+  Rs3Layout l;
+  l.D = n * n;
+  l.Dp = (l.D + 127) / 128 * 128;
+  l.Rq = (R + 127) / 128 * 128;
+  l.KC3 = l.Dp / sg::kCK;
+  l.MT = l.Dp / 128;
+  l.NT3 = l.Rq / 128;
+  l.MTo = n_obs > 0 ? (n_obs + 127) / 128 : 0;
+  l.apiece = (size_t)l.MT * l.KC3 * sg::kPiece;
+  l.epiece = (size_t)l.MTo * l.KC3 * sg::kPiece;
+  l.bpiece = (size_t)l.NT3 * l.KC3 * sg::kPiece;
+  l.tarr = (size_t)l.Rq * l.Dp * sizeof(float);
+  l.state = (size_t)2 * l.Rq * l.Dp * sizeof(float);
+  l.rows = (((size_t)3 * (l.MT + l.MTo) * 128 * sizeof(float)) + 1023) / 1024 * 1024;
+  // A: 3 products x 3 pieces (generator, observables); B: 2 buffers x 3
+  // operands x 2 pieces; T: 3 products x hi/lo; state hi, lo, accumulator
+  l.total = 9 * l.apiece + 9 * l.epiece + 12 * l.bpiece + 6 * l.tarr + 3 * l.state + l.rows + 4096;
+  return l;
+}
+
+}  // namespace
+
+extern "C" size_t lime_redfield_split3_workspace(int32_t n, int32_t n_rhs, int32_t n_obs) {
+  if (n <= 0 || n_rhs <= 0 || n_obs < 0) return 0;
+  return rs3_layout(n, n_rhs, n_obs).total;
+}
+
+extern "C" int lime_redfield_rk4_split3(const LimeRedfieldSplitDesc* d, void* stream) {
+  if (!d || d->n <= 0 || d->n_rhs <= 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (!d->R || !d->rho || !d->workspace || !d->status) return LIME_ERR_ARG;
+  if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
+  if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60) return LIME_ERR_ARG;
+  if ((int64_t)d->n * d->n > (1 << 20)) return LIME_ERR_UNSUPPORTED;
+  const Rs3Layout L = rs3_layout(d->n, d->n_rhs, d->n_obs);
+  if (d->workspace_bytes < L.total) return LIME_ERR_WORKSPACE;
+  if ((reinterpret_cast<uintptr_t>(d->workspace) & 1023) != 0) return LIME_ERR_ARG;
+  const int D = L.D, Dp = L.Dp, Rq = L.Rq, MT = L.MT, NT3 = L.NT3, MTo = L.MTo, KC3 = L.KC3;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t* w = reinterpret_cast<uint8_t*>(d->workspace);
+  uint8_t* AL[3][3];
+  uint8_t* AE[3][3];
+  for (int p = 0; p < 3; ++p)
+    for (int i = 0; i < 3; ++i) { AL[p][i] = w; w += L.apiece; }
+  for (int p = 0; p < 3; ++p)
+    for (int i = 0; i < 3; ++i) { AE[p][i] = w; w += L.epiece; }
+  uint8_t* B[2][3][2];
+  for (int c = 0; c < 2; ++c)
+    for (int p = 0; p < 3; ++p)
+      for (int i = 0; i < 2; ++i) { B[c][p][i] = w; w += L.bpiece; }
+  float* Thi[3];
+  float* Tlo[3];
+  for (int p = 0; p < 3; ++p) {
+    Thi[p] = reinterpret_cast<float*>(w); w += L.tarr;
+    Tlo[p] = reinterpret_cast<float*>(w); w += L.tarr;
+  }
+  float* Phi = reinterpret_cast<float*>(w); w += L.state;
+  float* Plo = reinterpret_cast<float*>(w); w += L.state;
+  float* Acc = reinterpret_cast<float*>(w); w += L.state;
+  float* rows = reinterpret_cast<float*>(w);
+  float* rinvL[3] = {rows, rows + (size_t)MT * 128, rows + (size_t)2 * MT * 128};
+  float* rinvE[3];
+  for (int p = 0; p < 3; ++p) rinvE[p] = rows + (size_t)3 * MT * 128 + (size_t)p * MTo * 128;
+  int64_t launches = 0;
+
+  for (int p = 0; p < 3; ++p) {
+    rsp::convert_real_rows_kernel<<<Dp, 256, 0, st>>>(reinterpret_cast<const double2*>(d->R), 0, p, d->n, D, D, KC3,
+                                                     AL[p][0], AL[p][1], AL[p][2], rinvL[p]);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+    if (MTo > 0) {
+      rsp::convert_real_rows_kernel<<<MTo * 128, 256, 0, st>>>(reinterpret_cast<const double2*>(d->obs_ops), 1, p,
+                                                              d->n, d->n_obs, D, KC3, AE[p][0], AE[p][1],
+                                                              AE[p][2], rinvE[p]);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+    }
+  }
+  const int obs_every = d->obs_every > 0 ? d->obs_every : 1;
+  if (MTo > 0) {
+    const size_t slots = (size_t)(d->n_steps / obs_every);
+    if (slots > 0) LIME_CUDA_TRY(cudaMemsetAsync(d->obs_out, 0, slots * d->n_rhs * d->n_obs * 2 * sizeof(double), st));
+  }
+
+  rsp::StageArgs a{};
+  a.Dp = Dp; a.W = 2 * Rq; a.KC = KC3; a.MT = MT; a.NT = NT3; a.Rp = Rq; a.R = d->n_rhs;
+  a.KS = 1; a.groups_per_split = KC3 / sg::kGroup;
+  a.sb = ldexpf(1.f, d->scale_b_log2);
+  a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
+  a.c_half = (float)(d->dt / 2.0);
+  a.c_full = (float)d->dt;
+  a.c_sixth = (float)(d->dt / 6.0);
+  a.c_sixth_lo = (float)(d->dt / 6.0 - (double)a.c_sixth);
+  a.Phi = Phi; a.Plo = Plo; a.Acc = Acc;
+  a.status = d->status;
+  a.max_wait = 1u << 26;
+  a.a_bytes = L.apiece; a.b_bytes = L.bpiece; a.st_floats = (size_t)Rq * Dp;
+  for (int p = 0; p < 3; ++p) {
+    for (int i = 0; i < 3; ++i) a.A3[p][i] = AL[p][i];
+    a.rinv3[p] = rinvL[p];
+    a.Thi3[p] = Thi[p];
+    a.Tlo3[p] = Tlo[p];
+  }
+  // the sum operand Sr + Si is held one power of two lower
+  a.inv_sb3[0] = a.inv_sb;
+  a.inv_sb3[1] = a.inv_sb;
+  a.inv_sb3[2] = 2.f * a.inv_sb;
+  rsp::Stage3 g{};
+  g.Rq = Rq;
+  g.KC3 = KC3;
+  g.sb_sum = 0.5f * a.sb;
+  g.b_bytes = L.bpiece;
+  for (int p = 0; p < 3; ++p) {
+    g.Thi[p] = Thi[p];
+    g.Tlo[p] = Tlo[p];
+  }
+  auto bind_next = [&](int c) {
+    for (int p = 0; p < 3; ++p)
+      for (int i = 0; i < 2; ++i) g.Bn[p][i] = B[c][p][i];
+  };
+  auto bind_cur = [&](rsp::StageArgs& x, int c) {
+    for (int p = 0; p < 3; ++p)
+      for (int i = 0; i < 2; ++i) x.B3c[p][i] = B[c][p][i];
+  };
+  const size_t runs = (size_t)Rq * (Dp / 8);
+  const int eb = (int)((runs + 255) / 256 < 65535 ? (runs + 255) / 256 : 65535);
+  bind_next(0);
+  rsp::init_state3_kernel<<<eb, 256, 0, st>>>(a, g, reinterpret_cast<const double2*>(d->rho), D, d->n_rhs);
+  LIME_CUDA_TRY(cudaGetLastError());
+  ++launches;
+
+  // observables: the three products with A = Etr, Eti, Etr + Eti; K split
+  // so that the grid covers the GPU about twice
+  rsp::StageArgs ao = a;
+  if (MTo > 0) {
+    int n_sm = 148, dev = 0;
+    LIME_CUDA_TRY(cudaGetDevice(&dev));
+    LIME_CUDA_TRY(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    ao.MT = MTo;
+    ao.a_bytes = L.epiece;
+    ao.n_obs = d->n_obs;
+    for (int p = 0; p < 3; ++p) {
+      for (int i = 0; i < 3; ++i) ao.A3[p][i] = AE[p][i];
+      ao.rinv3[p] = rinvE[p];
+    }
+    // <E> = (T1 - T2) + i (T3 - T1 - T2)
+    ao.obs_c3[0][0] = 1.f;  ao.obs_c3[0][1] = -1.f;
+    ao.obs_c3[1][0] = -1.f; ao.obs_c3[1][1] = -1.f;
+    ao.obs_c3[2][0] = 0.f;  ao.obs_c3[2][1] = 1.f;
+    const int groups = KC3 / sg::kGroup;
+    int ks = (2 * n_sm) / (3 * MTo * NT3);
+    ks = ks < 1 ? 1 : (ks > groups ? groups : ks);
+    ao.groups_per_split = (groups + ks - 1) / ks;
+    ao.KS = (groups + ao.groups_per_split - 1) / ao.groups_per_split;
+  }
+
+  const size_t smem = sg::kSmemBytes;
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int cur = 0;
+  for (int step = 0; step < d->n_steps; ++step) {
+    for (int s = 0; s < 4; ++s) {
+      a.stage = s;
+      bind_cur(a, cur);
+      rsp::gemm_kernel<4><<<3 * MT * NT3, sg::kThreads, smem, st>>>(a);
+      LIME_CUDA_TRY(cudaGetLastError());
+      bind_next(cur ^ 1);
+      rsp::stage3_kernel<<<eb, 256, 0, st>>>(a, g);
+      LIME_CUDA_TRY(cudaGetLastError());
+      launches += 2;
+      cur ^= 1;
+    }
+    if (MTo > 0 && ((step + 1) % obs_every) == 0) {
+      const int slot = (step + 1) / obs_every - 1;
+      bind_cur(ao, cur);
+      ao.obs = d->obs_out + (size_t)slot * d->n_rhs * d->n_obs * 2;
+      rsp::gemm_kernel<5><<<3 * ao.KS * MTo * NT3, sg::kThreads, smem, st>>>(ao);
+      LIME_CUDA_TRY(cudaGetLastError());
+      ++launches;
+    }
+  }
+  const int fb = (int)(((size_t)d->n_rhs * D + 255) / 256);
+  rsp::final_state_kernel<<<fb < 65535 ? fb : 65535, 256, 0, st>>>(Phi, Plo, Dp, Rq,
                                                                      reinterpret_cast<double2*>(d->rho), D, d->n_rhs);
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
@@ -882,14 +1278,13 @@ extern "C" int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d
     }
     const float* rho_after = step + 1 < S ? ys + (size_t)(step + 1) * 4 * stf : after;
     {
-      const dim3 sg_grid((Dp + 255) / 256, Rp / 8 < 8 ? Rp / 8 : 8);
-      rsp::adj_src_kernel<<<sg_grid, 256, (size_t)8 * (n_obs > 0 ? n_obs : 1) * sizeof(float2), st>>>(
-          Lhi, Llo, D, R, Dp, Rp, EtF, n_obs, g, lmax);
+      const dim3 sg_grid((Dp + rsp::kSrcTD - 1) / rsp::kSrcTD, (Rp + rsp::kSrcTR - 1) / rsp::kSrcTR);
+      rsp::adj_src_kernel<<<sg_grid, 256, 0, st>>>(Lhi, Llo, D, R, Dp, Rp, EtF, n_obs, g, lmax);
     }
     LIME_CUDA_TRY(cudaGetLastError());
     ++launches;
     if (g != nullptr && d->grad_obs != nullptr) {
-      const dim3 go_grid((D + 255) / 256, (n_obs + 7) / 8);
+      const dim3 go_grid((D + rsp::kGoTD - 1) / rsp::kGoTD, (n_obs + rsp::kGoTO - 1) / rsp::kGoTO);
       rsp::adj_grad_obs_kernel<<<go_grid, 256, 0, st>>>(
           rho_after, g, n_obs, n, R, Dp, Rp, reinterpret_cast<double2*>(d->grad_obs));
       LIME_CUDA_TRY(cudaGetLastError());

@@ -207,6 +207,10 @@ struct Tile {
   // a chunk past them is not copied, and the tile aborts)
   size_t a_avail = kNoExtent, b_avail = kNoExtent;
   int32_t* status = nullptr;
+  // park the two-sum words separately (mainloop): hi * scale into the ring
+  // tile, lo * scale in place in S.lo ([col][row], stride kBM), for callers
+  // that combine tiles with cancellation
+  int park_split = 0;
 };
 
 // TMEM allocation and barrier set-up; every thread of the CTA calls it.
@@ -381,31 +385,228 @@ __device__ __forceinline__ bool mainloop(Smem& S, const Tile& T) {
   const float rs = __fmul_rn(T.row_inv[r], T.inv_sb);
   float* ft = S.tile();
   if (ok) {
+    if (T.park_split) {
 #pragma unroll
-    for (int c = 0; c < kEpiCols; ++c) ft[(kEpiCols * h + c) * kFStride + r] = __fmul_rn(__fadd_rn(hi[c], lo[c * kBM]), rs);
+      for (int c = 0; c < kEpiCols; ++c) {
+        ft[(kEpiCols * h + c) * kFStride + r] = __fmul_rn(hi[c], rs);
+        lo[c * kBM] = __fmul_rn(lo[c * kBM], rs);
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < kEpiCols; ++c)
+        ft[(kEpiCols * h + c) * kFStride + r] = __fmul_rn(__fadd_rn(hi[c], lo[c * kBM]), rs);
+    }
   }
   epi_bar();
   return true;
 }
 
+// ---------------------------------------------------------------- tile sequences
+// A persistent CTA runs a sequence of tiles in one launch and keeps the
+// ring, the TMEM accumulators and their barriers from tile to tile: the
+// chunk counter gc and the accumulator-group counter gp run on across
+// tiles, so the producer and the MMA issuer start the next tile's copies and
+// its first two 128-K groups (the double-buffered D0/D1) while the epilogue
+// warps are still in the previous tile's fused epilogue.  The finished tile
+// is parked in place in the two-sum buffer S.lo (the ring by then holds the
+// next tile's operands), in a swizzled layout (park_idx): a drain writes 32
+// consecutive rows of one column per warp, a fused epilogue reads 8-row runs
+// of 8 columns, both without bank conflicts.
+struct Seq {
+  int gc = 0;   // chunks issued (producer) / consumed (MMA issuer) so far
+  int gp = 0;   // 128-K accumulator groups committed (MMA issuer) / drained (epilogue) so far
+};
+
+__host__ __device__ __forceinline__ int park_idx(int col, int row) { return col * kBM + (row ^ ((col & 7) << 2)); }
+
+// parked rows row..row+7 (row % 8 == 0) of column col
+__device__ __forceinline__ void ld8_park(const float* ft, int col, int row, float (&v)[8]) {
+  const int sw = (col & 7) << 2;
+  const float4 x = *reinterpret_cast<const float4*>(ft + col * kBM + (row ^ sw));
+  const float4 y = *reinterpret_cast<const float4*>(ft + col * kBM + ((row + 4) ^ sw));
+  v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w; v[4] = y.x; v[5] = y.y; v[6] = y.z; v[7] = y.w;
+}
+
+// named barrier of the epilogue warps that also ORs a predicate over them
+__device__ __forceinline__ bool epi_bar_or(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "barrier.cta.red.or.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(kEpiThreads)
+      : "memory");
+  return r != 0;
+}
+
+// bounded wait that also gives up once another role of the CTA has aborted
+// (checked every 256 polls), so one expired wait ends the whole sequence
+__device__ __forceinline__ bool seq_wait(Smem& S, uint64_t* bar, uint32_t parity, uint32_t max_iters) {
+  for (uint32_t it = 0; it < max_iters; ++it) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if ((it & 255u) == 255u && *(volatile int*)&S.abort) return false;
+  }
+  return false;
+}
+
+// producer (warp 0, lane 0): the bulk copies of the tile's chunks.  False
+// once the CTA aborts (a wait expired, or a chunk past an operand's extent).
+__device__ __forceinline__ bool seq_produce(Smem& S, const Tile& T, Seq& q) {
+  for (int c = 0; c < T.n_chunks; ++c, ++q.gc) {
+    const int s = q.gc % kStages;
+    const uint32_t ph = (uint32_t)(q.gc / kStages) & 1u;
+    if (!seq_wait(S, &S.empty[s], ph ^ 1u, T.max_wait)) { atomicExch(&S.abort, 1); return false; }
+    if (*(volatile int*)&S.abort) return false;
+    if (!in_bounds((size_t)(T.c0 + c) * kPiece, kPiece, T.a_avail, T.status) ||
+        !in_bounds((size_t)(T.c0 + c) * kPiece, kPiece, T.b_avail, T.status)) {
+      atomicExch(&S.abort, 1);
+      return false;
+    }
+    tc::mbar_arrive_expect_tx(&S.full[s], 5 * kPiece);
+    const size_t off = (size_t)(T.c0 + c) * kPiece;
+    tc::bulk_g2s(S.stage[s][0], T.A[0] + off, kPiece, &S.full[s]);
+    tc::bulk_g2s(S.stage[s][1], T.A[1] + off, kPiece, &S.full[s]);
+    tc::bulk_g2s(S.stage[s][2], T.A[2] + off, kPiece, &S.full[s]);
+    tc::bulk_g2s(S.stage[s][3], T.B[0] + off, kPiece, &S.full[s]);
+    tc::bulk_g2s(S.stage[s][4], T.B[1] + off, kPiece, &S.full[s]);
+  }
+  return true;
+}
+
+// producer, after its last tile: the copies still in flight have landed
+__device__ __forceinline__ void seq_produce_end(Smem& S, const Seq& q, uint32_t max_wait) {
+  for (int c = q.gc - 1; c >= 0 && c >= q.gc - kStages; --c)
+    tc::mbar_wait_bounded(&S.full[c % kStages], (uint32_t)(c / kStages) & 1u, max_wait);
+}
+
+// MMA issuer (warp 1, lane 0): the tile's MMAs, one accumulator group per
+// 128 K into D0/D1 buffer gp & 1.
+__device__ __forceinline__ bool seq_mma(Smem& S, const Tile& T, Seq& q) {
+  constexpr uint32_t idesc = tc::idesc_f16(kBM, kBN, 0);
+  const uint32_t tbase = S.tmem_base;
+  for (int c = 0; c < T.n_chunks; ++c, ++q.gc) {
+    const int s = q.gc % kStages;
+    const uint32_t ph = (uint32_t)(q.gc / kStages) & 1u;
+    const int b = q.gp & 1;
+    const bool first = (c % kGroup) == 0;
+    const bool last = (c % kGroup) == kGroup - 1;
+    if (!seq_wait(S, &S.full[s], ph, T.max_wait)) { atomicExch(&S.abort, 1); return false; }
+    if (first && !seq_wait(S, &S.acce[b], ((uint32_t)(q.gp >> 1) & 1u) ^ 1u, T.max_wait)) {
+      atomicExch(&S.abort, 1);
+      return false;
+    }
+    if (*(volatile int*)&S.abort) return false;
+    tc::tc_fence_after();
+    const uint32_t d0 = tbase + (uint32_t)(2 * b) * 128u;
+    const uint32_t d1 = d0 + 128u;
+    const uint32_t base = tc::smem_u32(S.stage[s][0]);
+#pragma unroll
+    for (int ks = 0; ks < kCK / 16; ++ks) {
+      const uint32_t ko = (uint32_t)ks * 2u * kLBO;
+      const uint64_t a0 = tc::smem_desc_noswizzle(base + 0 * kPiece + ko, kLBO, kSBO);
+      const uint64_t a1 = tc::smem_desc_noswizzle(base + 1 * kPiece + ko, kLBO, kSBO);
+      const uint64_t a2 = tc::smem_desc_noswizzle(base + 2 * kPiece + ko, kLBO, kSBO);
+      const uint64_t b0 = tc::smem_desc_noswizzle(base + 3 * kPiece + ko, kLBO, kSBO);
+      const uint64_t b1 = tc::smem_desc_noswizzle(base + 4 * kPiece + ko, kLBO, kSBO);
+      const uint32_t acc = (first && ks == 0) ? 0u : 1u;
+      tc::mma_f16_ss(d0, a0, b0, idesc, acc);
+      tc::mma_f16_ss(d1, a1, b0, idesc, acc);
+      tc::mma_f16_ss(d1, a0, b1, idesc, 1u);
+      tc::mma_f16_ss(d1, a1, b1, idesc, 1u);
+      tc::mma_f16_ss(d1, a2, b0, idesc, 1u);
+    }
+    tc::mma_commit(&S.empty[s]);
+    if (last) {
+      tc::mma_commit(&S.accf[b]);
+      ++q.gp;
+    }
+  }
+  return true;
+}
+
+// MMA issuer, after its last tile: every MMA has completed before TMEM is released
+__device__ __forceinline__ void seq_mma_end(Smem& S, uint32_t max_wait) {
+  tc::mma_commit(&S.drain);
+  tc::mbar_wait_bounded(&S.drain, 0u, max_wait);
+}
+
+// epilogue warps: drain the tile's accumulator groups into the fp32 two-sum
+// and park C[r][c] * row_inv[r] * inv_sb at S.lo[park_idx(c, r)]; ends with
+// a named barrier of the epilogue warps.  The caller must have passed an
+// epilogue barrier after reading the previous parked tile.  False if a wait
+// expired (the tile is not valid).
+__device__ __forceinline__ bool seq_drain(Smem& S, const Tile& T, Seq& q) {
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int lq = warp & 3;
+  const int h = (warp - 2) >> 2;
+  const int r = lq * 32 + lane;
+  const uint32_t lane_addr = S.tmem_base + ((uint32_t)(lq * 32) << 16);
+  float hi[kEpiCols];
+#pragma unroll
+  for (int c = 0; c < kEpiCols; ++c) {
+    hi[c] = 0.f;
+    S.lo[park_idx(kEpiCols * h + c, r)] = 0.f;
+  }
+  const int n_groups = T.n_chunks / kGroup;
+  bool ok = true;
+  for (int p = 0; p < n_groups; ++p, ++q.gp) {
+    const int b = q.gp & 1;
+    if (!seq_wait(S, &S.accf[b], (uint32_t)(q.gp >> 1) & 1u, T.max_wait)) {
+      atomicExch(&S.abort, 1);
+      ok = false;
+      break;
+    }
+    tc::tc_fence_after();
+    const uint32_t d0 = lane_addr + (uint32_t)(2 * b) * 128u + (uint32_t)(kEpiCols * h);
+#pragma unroll
+    for (int qq = 0; qq < kEpiCols / 16; ++qq) {
+      float v[16], er[16];
+      tc::tmem_ld16(d0 + 16 * qq, v);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const float x = v[e];
+        const float sm = __fadd_rn(hi[16 * qq + e], x);
+        const float bv = __fsub_rn(sm, hi[16 * qq + e]);
+        er[e] = __fadd_rn(__fsub_rn(hi[16 * qq + e], __fsub_rn(sm, bv)), __fsub_rn(x, bv));
+        hi[16 * qq + e] = sm;
+      }
+      tc::tmem_ld16(d0 + 128u + 16 * qq, v);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        float* l = S.lo + park_idx(kEpiCols * h + 16 * qq + e, r);
+        *l = __fadd_rn(*l, __fadd_rn(er[e], v[e]));
+      }
+    }
+    tc::tc_fence_before();
+    tc::mbar_arrive(&S.acce[b]);
+  }
+  if (ok) {
+    const float rs = __fmul_rn(T.row_inv[r], T.inv_sb);
+#pragma unroll
+    for (int c = 0; c < kEpiCols; ++c) {
+      float* l = S.lo + park_idx(kEpiCols * h + c, r);
+      *l = __fmul_rn(__fadd_rn(hi[c], *l), rs);
+    }
+  }
+  epi_bar();
+  return ok;
+}
+
 // ---------------------------------------------------------------- operand conversion
-// A pieces of one row (row = blockIdx.x) of the real block row [Mr | Mi] of
-// a complex matrix M (rows x cols, row stride ld; element (row, kk) read by
-// elem).  The row is scaled by the power of two that brings its largest
-// component into [2^12, 2^13) and split as A0 = 64 k (|k| <= 127) + fp16
-// residuals A1, A2; row_inv gets the inverse scale (0 for padding rows and
-// all-zero rows).  Columns kk >= cols are zero; Kp is the padded column
-// count (the imaginary block starts at Kp), KC the chunks per row tile.
-template <class Elem>
-__device__ __forceinline__ void convert_row(const Elem& elem, int row, bool valid, int cols, int Kp, int KC,
-                                            uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
+// A pieces of one row of a real operand whose K entries are value(k), k in
+// [0, Ktot) (zero where the operand is padded).  The row is scaled by the
+// power of two that brings its largest entry into [2^12, 2^13) and split as
+// A0 = 64 k (|k| <= 127) + fp16 residuals A1, A2; row_inv gets the inverse
+// scale (0 for padding rows and all-zero rows).  KC: chunks per row tile.
+template <class Val>
+__device__ __forceinline__ void convert_row_values(const Val& value, int row, bool valid, int Ktot, int KC,
+                                                   uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
   __shared__ double red[32];
   double mx = 0.0;
   if (valid)
-    for (int k = threadIdx.x; k < cols; k += blockDim.x) {
-      const double2 z = elem(k);
-      mx = fmax(mx, fmax(fabs(z.x), fabs(z.y)));
-    }
+    for (int k = threadIdx.x; k < Ktot; k += blockDim.x) mx = fmax(mx, fabs(value(k)));
   for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
   __syncthreads();
@@ -423,15 +624,8 @@ __device__ __forceinline__ void convert_row(const Elem& elem, int row, bool vali
     if (sh > 140 || sh < -140) live = false;
   }
   if (threadIdx.x == 0) row_inv[row] = live ? ldexpf(1.f, -sh) : 0.f;
-  for (int k = threadIdx.x; k < 2 * Kp; k += blockDim.x) {
-    double x = 0.0;
-    if (live) {
-      const int kk = k < Kp ? k : k - Kp;
-      if (kk < cols) {
-        const double2 z = elem(kk);
-        x = ldexp(k < Kp ? z.x : z.y, sh);
-      }
-    }
+  for (int k = threadIdx.x; k < Ktot; k += blockDim.x) {
+    const double x = live ? ldexp(value(k), sh) : 0.0;
     const double kq = fmin(fmax(rint(x * (1.0 / 64.0)), -kA0Max), kA0Max);
     const double v0 = kq * 64.0;
     const double r1 = x - v0;
@@ -442,6 +636,21 @@ __device__ __forceinline__ void convert_row(const Elem& elem, int row, bool vali
     *reinterpret_cast<__half*>(A1 + off) = h1;
     *reinterpret_cast<__half*>(A2 + off) = h2;
   }
+}
+
+// A pieces of one row of the real block row [Mr | Mi] of a complex matrix M
+// (element (row, kk) read by elem, kk < cols; columns kk >= cols are zero;
+// Kp is the padded column count, where the imaginary block starts).
+template <class Elem>
+__device__ __forceinline__ void convert_row(const Elem& elem, int row, bool valid, int cols, int Kp, int KC,
+                                            uint8_t* A0, uint8_t* A1, uint8_t* A2, float* row_inv) {
+  auto value = [&](int k) -> double {
+    const int kk = k < Kp ? k : k - Kp;
+    if (kk >= cols) return 0.0;
+    const double2 z = elem(kk);
+    return k < Kp ? z.x : z.y;
+  };
+  convert_row_values(value, row, valid, 2 * Kp, KC, A0, A1, A2, row_inv);
 }
 
 }  // namespace sg

@@ -465,7 +465,7 @@ def split_operands_mdiag(gen: LindbladGenerator):
 
 def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
                 obs_every: int, param_batch: int, events=None, max_retries: int = 3, drive=None,
-                defer: bool = False):
+                defer: bool = False, sink=None):
     """Any generator on the tensor cores (``lime_lindblad_rk4_stream``):
     streaming split-precision GEMMs for Heff rho and sum_k L_k rho L_k^dag.
     State scale: max |rho0| * 1.25 <= 2^13; L_k rho scale from the largest
@@ -475,7 +475,11 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     ``redo()`` relaunches with 4x smaller scales and returns the new
     (obs, status, rho).  With ``defer=True`` the range check is left to the
     caller (no host synchronisation after the launch, so launches on other
-    streams are enqueued without waiting); otherwise it is done here."""
+    streams are enqueued without waiting); otherwise it is done here.
+    ``sink``: a list that receives the descriptor (with the buffers it
+    points to) instead of launching it, for one grouped launch of several
+    propagations (``lime_lindblad_rk4_stream_groups``); implies defer, and
+    retries relaunch the propagation on its own."""
     lib = nat.require_device()
     B, n = rho.shape[0], gen.n
     dev = rho.device
@@ -509,7 +513,7 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     aligned = (ws.data_ptr() + 1023) // 1024 * 1024
     start = rho.contiguous()
 
-    def launch():
+    def launch(alone=False):
         work = start.clone()
         status.zero_()
         d = nat.LindbladStreamDesc()
@@ -533,6 +537,9 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
         if drive is not None:
             ops, coef = drive
             d.n_drive, d.drive_ops, d.drive_coef = ops.shape[0], ops.data_ptr(), coef.data_ptr()
+        if sink is not None and not alone:
+            sink.append((d, (work, start, ws, obs_out, status, E, m_diag, gen)))
+            return work
         if events is not None:
             events[0].record()
         nat.check(lib.lime_lindblad_rk4_stream(d, _stream_ptr()), 'lime_lindblad_rk4_stream')
@@ -543,10 +550,10 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     def redo():
         scales[0] -= 2
         scales[1] -= 2
-        return obs_out[:, :n_slots, :n_obs], status, launch()
+        return obs_out[:, :n_slots, :n_obs], status, launch(alone=True)
 
     work = launch()
-    if not defer:
+    if not defer and sink is None:
         for _ in range(max_retries):
             if not int(status.item()) & nat.LIME_FLAG_RANGE:
                 break
@@ -566,7 +573,7 @@ def _host_hermitian(rho0):
 def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
             states_every: int = 0, precision: str = 'fp64', trace_tol: float | None = None,
             obs_every: int = 1, events=None, drive=None, defer: bool = False,
-            hermitian: bool | None = None):
+            hermitian: bool | None = None, stream_sink=None):
     """Enqueue one propagation on the current stream; returns a closure that
     checks the status word (synchronising the stream) and assembles
     ``(obs, states, rho)``.  ``defer``: nothing after the launch waits for
@@ -576,7 +583,9 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     two Hermitian parts.  Hermiticity is checked on the host for host
     inputs; for a device tensor the batched split kernel checks it itself
     (LIME_FLAG_NOT_HERMITIAN, after which the closure reruns the two parts),
-    the other paths compare rho0 with its adjoint on the device."""
+    the other paths compare rho0 with its adjoint on the device.
+    ``stream_sink``: see ``_run_stream`` (a propagation on the streaming
+    path is collected there instead of launched)."""
     if obs_every < 1 or states_every < 0 or n_steps < 0:
         raise ValueError('obs_every must be >= 1, states_every >= 0, n_steps >= 0')
     device = gen.heff.device
@@ -628,7 +637,7 @@ def _launch(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     else:
         o, s, status, work, redo = _run_stream(gen, work, dt, n_steps, expand_e_ops(e_ops, n), obs_every,
                                                param_batch=B, events=events, drive=drive,
-                                               defer=defer)
+                                               defer=defer, sink=stream_sink)
 
     def finish(check: bool = True):
         nonlocal o, status, work
@@ -731,10 +740,12 @@ class RaggedGroup:
         return out
 
 
-def ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision: str, device) -> list:
+def ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision: str, device,
+                  pack: bool = True) -> list:
     """Group an uneven batch by (dimension, operator count) and build each
     group's generator, states and observables on ``device`` (packed
-    block-diagonally for precision='split' and n <= 32)."""
+    block-diagonally for precision='split' and n <= 32 unless ``pack`` is
+    False)."""
     groups = {}
     for i in range(len(H_list)):
         h = H_list[i]
@@ -743,7 +754,7 @@ def ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision: str, dev
     out = []
     for (n, K), idx in sorted(groups.items()):
         m = len(e_ops_list[idx[0]])
-        p = pack_count(n, precision)
+        p = pack_count(n, precision) if pack else 1
 
         def stacked(get):
             x = torch.stack([as_device(get(i), device) for i in idx])
@@ -775,22 +786,103 @@ def ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision: str, dev
     return out
 
 
+UNEVEN_DEFAULT = {'mode': 'groups', 'order': 1, 'n_ctas': 0, 'pack': True}
+UNEVEN_CANDIDATES = (
+    {'mode': 'groups', 'order': 1, 'n_ctas': 0, 'pack': True},
+    {'mode': 'groups', 'order': 0, 'n_ctas': 0, 'pack': True},
+    {'mode': 'groups', 'order': 1, 'n_ctas': 0, 'pack': False},
+    {'mode': 'streams', 'order': 1, 'n_ctas': 0, 'pack': True},
+    {'mode': 'streams', 'order': 1, 'n_ctas': 0, 'pack': False},
+)
+
+
+def _ragged_dims(H_list, c_ops_list):
+    """(dimension, operator count) -> instance count of an uneven batch."""
+    cnt = {}
+    for i, h in enumerate(H_list):
+        n = int(h.shape[-1]) if hasattr(h, 'shape') else int(np.shape(h)[-1])
+        k = (n, len(c_ops_list[i]))
+        cnt[k] = cnt.get(k, 0) + 1
+    return cnt
+
+
+def uneven_class(H_list, c_ops_list, precision: str, pack: bool = True) -> str:
+    """The autotuner's N-class of an uneven batch (``tuning.uneven_class``
+    over the groups the streaming path would launch)."""
+    from . import tuning
+    dims, counts, ks = [], [], set()
+    for (n, K), c in sorted(_ragged_dims(H_list, c_ops_list).items()):
+        p = pack_count(n, precision) if pack else 1
+        dims.append((n * p + 63) // 64 * 64)
+        counts.append(-(-c // p))
+        ks.add(K)
+    return tuning.uneven_class(dims, counts, max(ks) if ks else 0)
+
+
+def ragged_enqueue(groups, dt: float, n_steps: int, precision: str, schedule=None, states_every: int = 0,
+                   trace_tol: float | None = None, obs_every: int = 1, device=None):
+    """Enqueue the propagation of prepared uneven-batch groups
+    (``ragged_groups``) on the current stream and return one finishing
+    closure per group (``closure(check) -> (obs, states, rho)``).
+
+    ``schedule['mode']``: 'groups' runs every group on the streaming
+    tensor-core path in one ``lime_lindblad_rk4_stream_groups`` call (per
+    stage one persistent launch for the GEMM 1 tiles of all groups and one
+    for the GEMM 2 tiles; ``order`` and ``n_ctas`` as there), the other
+    groups (batched kernel, FP64) one after another; 'streams' runs each
+    group's launch sequence on its own CUDA stream."""
+    sched = dict(UNEVEN_DEFAULT if schedule is None else schedule)
+    device = _dev(device)
+    main = torch.cuda.current_stream(device)
+    fins = []
+    if sched.get('mode') == 'groups' and precision == 'split':
+        sink = []
+        for grp in groups:
+            fins.append(_launch(grp.gen, grp.rho, dt, n_steps, grp.e_ops, states_every=states_every,
+                                precision=precision, trace_tol=trace_tol, obs_every=obs_every, defer=True,
+                                stream_sink=sink))
+        if sink:
+            lib = nat.require_device()
+            cap = int(lib.lime_lindblad_stream_max_groups())
+            for c0 in range(0, len(sink), cap):
+                part = sink[c0:c0 + cap]
+                arr = (nat.LindbladStreamDesc * len(part))(*[d for d, _ in part])
+                nat.check(lib.lime_lindblad_rk4_stream_groups(arr, len(part), int(sched.get('n_ctas', 0)),
+                                                              int(sched.get('order', 1)), _stream_ptr()),
+                          'lime_lindblad_rk4_stream_groups')
+        return fins
+    streams = []
+    for grp in groups:
+        st = torch.cuda.Stream(device=device)
+        st.wait_stream(main)
+        with torch.cuda.stream(st):
+            fins.append(_launch(grp.gen, grp.rho, dt, n_steps, grp.e_ops, states_every=states_every,
+                                precision=precision, trace_tol=trace_tol, obs_every=obs_every, defer=True))
+        streams.append(st)
+    for st in streams:
+        main.wait_stream(st)
+    return fins
+
+
 def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None,
                      e_ops_list=None, states_every: int = 0, precision: str = 'fp64',
-                     trace_tol: float | None = None, obs_every: int = 1, device=None):
+                     trace_tol: float | None = None, obs_every: int = 1, device=None,
+                     schedule=None):
     """Uneven batch: instance i has its own Hamiltonian H_list[i] (n_i x n_i),
     collapse operators c_ops_list[i] and observables e_ops_list[i] (lists of
     n_i x n_i operators; every instance has the same number of observables).
 
     Instances with equal dimension and operator counts are stacked into one
-    batched launch (with precision='split', chains of dimension <= 32 are
-    packed block-diagonally, 64 // n to an instance); the launches of
-    different dimensions run concurrently on separate CUDA streams and the
-    status words are checked once all are enqueued.  ``precision``: 'fp64'
-    or 'split' (the batched tensor-core kernel where it applies, the
-    streaming tensor-core GEMMs elsewhere).  Returns three lists in input
-    order: observables (n_steps // obs_every, n_obs), states or None, final
-    rho.
+    batched propagation (with precision='split', chains of dimension <= 32
+    are packed block-diagonally, 64 // n to an instance).  With
+    precision='split' the groups on the streaming tensor-core path run in
+    lockstep, per RK4 stage one persistent launch for all groups' GEMM 1
+    tiles and one for their GEMM 2 tiles (``ragged_enqueue``); the
+    schedule is the autotuner's cached choice for this batch's N-class
+    (``tuning``, ``autotune_ragged``) or ``UNEVEN_DEFAULT``, unless given.
+    Status words are checked once everything is enqueued.  ``precision``:
+    'fp64' or 'split'.  Returns three lists in input order: observables
+    (n_steps // obs_every, n_obs), states or None, final rho.
     """
     B = len(H_list)
     if len(rho0_list) != B:
@@ -803,20 +895,59 @@ def propagate_ragged(H_list, rho0_list, dt: float, n_steps: int, c_ops_list=None
     if len(n_obs) > 1:
         raise ValueError('every instance needs the same number of observables')
     device = _dev(device)
-    main = torch.cuda.current_stream(device)
-    pending = []
-    for grp in ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision, device):
-        st = torch.cuda.Stream(device=device)
-        st.wait_stream(main)
-        with torch.cuda.stream(st):
-            fin = _launch(grp.gen, grp.rho, dt, n_steps, grp.e_ops, states_every=states_every,
-                          precision=precision, trace_tol=trace_tol, obs_every=obs_every, defer=True)
-        pending.append((grp, st, fin))
+    if schedule is None:
+        from . import tuning
+        schedule = UNEVEN_DEFAULT
+        if precision == 'split':
+            schedule = tuning.choose('lindblad_uneven', uneven_class(H_list, c_ops_list, precision),
+                                     precision, UNEVEN_DEFAULT, arch=tuning.arch_tag(device))
+    groups = ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision, device,
+                           pack=bool(schedule.get('pack', True)))
+    fins = ragged_enqueue(groups, dt, n_steps, precision, schedule, states_every=states_every,
+                          trace_tol=trace_tol, obs_every=obs_every, device=device)
     obs, states, rhos = [None] * B, [None] * B, [None] * B
-    for grp, st, fin in pending:
-        main.wait_stream(st)
-        with torch.cuda.stream(st):
-            res = grp.unpack(*fin(True))
+    for grp, fin in zip(groups, fins):
+        res = grp.unpack(*fin(True))
         for i, (o, s, r) in zip(grp.idx, res):
             obs[i], states[i], rhos[i] = o, s, r
     return obs, states, rhos
+
+
+def autotune_ragged(H_list, rho0_list, dt: float, c_ops_list=None, e_ops_list=None, precision: str = 'split',
+                    steps: int = 8, candidates=UNEVEN_CANDIDATES, device=None, cache=None, force: bool = False):
+    """Time every candidate schedule of ``propagate_ragged`` on this batch
+    (GPU time of ``steps`` RK4 steps minus that of ``steps // 2``, so the
+    per-call operand conversion cancels; CUDA events) and store the fastest
+    in the tuning cache under the batch's N-class.  Returns
+    ``(choice, times)`` (times None when the cache already held the key)."""
+    from . import tuning
+    B = len(H_list)
+    c_ops_list = [[] for _ in range(B)] if c_ops_list is None else list(c_ops_list)
+    e_ops_list = [[] for _ in range(B)] if e_ops_list is None else list(e_ops_list)
+    device = _dev(device)
+    prepared = {}
+
+    def measure(cand):
+        pack = bool(cand.get('pack', True))
+        if pack not in prepared:
+            prepared[pack] = ragged_groups(H_list, rho0_list, c_ops_list, e_ops_list, precision, device,
+                                           pack=pack)
+        groups = prepared[pack]
+
+        def run(k):
+            main = torch.cuda.current_stream(device)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(device)
+            a.record(main)
+            fins = ragged_enqueue(groups, dt, k, precision, cand, device=device)
+            b.record(main)
+            torch.cuda.synchronize(device)
+            for f in fins:
+                f(True)
+            return a.elapsed_time(b) / 1e3
+
+        run(1)
+        return (run(steps) - run(max(1, steps // 2))) / (steps - max(1, steps // 2))
+
+    return tuning.tune('lindblad_uneven', uneven_class(H_list, c_ops_list, precision), precision, candidates,
+                       measure, arch=tuning.arch_tag(device), cache=cache, force=force)

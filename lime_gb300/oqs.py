@@ -28,8 +28,21 @@ from .engine import DiagonalOps, Populations, SiteDephasing  # noqa: F401  (publ
 from .result import Result
 
 
+_PINNED_MIN_BYTES = 1 << 20
+
+
 def _np(t):
-    return t.detach().cpu().numpy()
+    """Host ndarray of a result tensor.  Large device results are copied into
+    page-locked memory from torch's caching host allocator (a pageable
+    destination makes the driver stage the copy through a bounce buffer at a
+    fraction of the link's rate); the array keeps that block alive, and the
+    block returns to the cache when the array is released."""
+    t = t.detach()
+    if t.device.type != 'cuda' or t.numel() * t.element_size() < _PINNED_MIN_BYTES:
+        return t.cpu().numpy()
+    out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    out.copy_(t.resolve_conj())
+    return out.numpy()
 
 
 def _squeeze_batch(x, batched):

@@ -171,10 +171,16 @@ def _pow2_floor(x: float) -> int:
     return int(np.floor(np.log2(x)))
 
 
+SPLIT_PRODUCT = '4m'   # complex product of the tensor-core Redfield RK4 ('3m' or '4m')
+
+
 def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=None, obs_every=1,
-                        max_retries=3):
+                        max_retries=3, product=None):
     """Tensor-core split-precision RK4 (``lime_redfield_rk4_split``) of
     eigenbasis density matrices (B, n, n) under the dense generator.
+    ``product``: '4m' (the real block form of the complex product) or '3m'
+    (three real products, ``lime_redfield_rk4_split3``); default
+    ``SPLIT_PRODUCT``.
 
     Same returns as ``propagate_vec`` without states.  The states are
     scaled to max |rho0| * 1.25 <= 2^13 (a power of two, so the scaling is
@@ -195,7 +201,12 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
     n_slots = n_steps // obs_every
     pmax = float(torch.view_as_real(rho0_eb).abs().max().item()) if rho0_eb.numel() else 0.0
     sb = _pow2_floor(8192.0 / (1.25 * pmax)) if pmax > 0 else 0
-    wsb = lib.lime_redfield_split_workspace(n, B, n_obs)
+    product = SPLIT_PRODUCT if product is None else product
+    if product not in ('3m', '4m'):
+        raise ValueError("product must be '3m' or '4m'")
+    name = 'lime_redfield_rk4_split3' if product == '3m' else 'lime_redfield_rk4_split'
+    run = getattr(lib, name)
+    wsb = (lib.lime_redfield_split3_workspace if product == '3m' else lib.lime_redfield_split_workspace)(n, B, n_obs)
     ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
     base = ws.data_ptr()
     aligned = (base + 1023) // 1024 * 1024
@@ -213,13 +224,13 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
             d.obs_ops, d.obs_out = E.data_ptr(), obs.data_ptr()
         d.workspace, d.workspace_bytes = aligned, wsb
         d.status = status.data_ptr()
-        nat.check(lib.lime_redfield_rk4_split(d, engine._stream_ptr()), 'lime_redfield_rk4_split')
+        nat.check(run(d, engine._stream_ptr()), name)
         flags = int(status.item())
         if flags & nat.LIME_FLAG_RANGE and attempt < max_retries:
             sb -= 2
             continue
         if flags:
-            raise nat.KernelFlagError(flags, 'lime_redfield_rk4_split')
+            raise nat.KernelFlagError(flags, name)
         break
     o = obs[:n_slots, :, :n_obs].permute(1, 0, 2)
     return o, None, P.reshape(B, n, n)
