@@ -318,6 +318,11 @@ int lime_redfield_adjoint_f64(const LimeRedfieldAdjointDesc* d, void* stream);
  *   workspace lime_redfield_split_workspace(n, n_rhs, n_obs) bytes,
  *            1024-byte aligned
  *   status   device int32 (LIME_FLAG_* bits)
+ *   stage_out  NULL, or fp32 [4 n_steps + 1][2 Rp][Dp] (Rp = n_rhs rounded
+ *            up to 64, Dp = n^2 rounded up to 128): every stage input of
+ *            the call and the final state, component-planar, in the layout
+ *            lime_redfield_adjoint_split takes as stage_in (the block form
+ *            only; lime_redfield_rk4_split3 rejects it)
  */
 typedef struct {
   int32_t n, n_rhs, n_steps, n_obs, obs_every;
@@ -329,6 +334,7 @@ typedef struct {
   double* obs_out;
   void* workspace;        size_t workspace_bytes;
   int32_t* status;
+  float* stage_out;
 } LimeRedfieldSplitDesc;
 
 size_t lime_redfield_split_workspace(int32_t n, int32_t n_rhs, int32_t n_obs);
@@ -360,7 +366,11 @@ int lime_redfield_rk4_split3(const LimeRedfieldSplitDesc* d, void* stream);
  *   obs_ops, obs_grad, grad_R, grad_obs as in lime_redfield_adjoint_f64
  *   status    device int32: LIME_FLAG_RANGE (repeat with a larger margin)
  *   workspace lime_redfield_adjoint_split_workspace(n, n_rhs, seg_steps,
- *             n_obs) bytes, 1024-byte aligned */
+ *             n_obs) bytes, 1024-byte aligned
+ *   stage_in  NULL (recompute the segment from ckpt), or the segment's
+ *             stage inputs as written by lime_redfield_rk4_split's stage_out
+ *             when it propagated this segment from ckpt with the same
+ *             scale_b_log2 (the recompute is skipped; same results) */
 typedef struct {
   int32_t n, n_rhs, seg_steps, step0, n_obs, obs_every, n_slots;
   int32_t scale_b_log2, margin_log2;
@@ -374,6 +384,7 @@ typedef struct {
   double* grad_obs;
   void* workspace;        size_t workspace_bytes;
   int32_t* status;
+  const float* stage_in;
 } LimeRedfieldAdjointSplitDesc;
 
 size_t lime_redfield_adjoint_split_workspace(int32_t n, int32_t n_rhs, int32_t seg_steps, int32_t n_obs);
@@ -582,11 +593,16 @@ typedef struct {
    * rho_out       [B][n][n] final state (NULL: written over rho)
    * auto_scale_b  1: each instance takes its B scale from its own rho(0),
    *               2^b sqrt(n) ||rho(0)||_F <= 2^13 (scale_b_log2 ignored)
+   * chunk_steps   RK4 steps per launch (0: about 2^22 instance-steps per
+   *               launch), rounded up to a multiple of obs_every; each
+   *               launch continues from the state the previous one wrote
+   *               to rho_out
    * Every instance's rho(0) is checked for Hermiticity on the float pair of
    * each element; a non-Hermitian one raises LIME_FLAG_NOT_HERMITIAN. */
   const void* a_pieces;   int64_t a_stride;
   double* rho_out;
   int32_t auto_scale_b;
+  int32_t chunk_steps;
 } LimeLindbladSplitDesc;
 
 size_t lime_lindblad_split_workspace(int32_t n, int32_t param_batch, int32_t n_drive, int32_t n_steps);

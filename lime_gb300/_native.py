@@ -99,7 +99,7 @@ class SplitDesc(ctypes.Structure):
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
                 ('a_pieces', c_void_p), ('a_stride', c_int64),
                 ('rho_out', c_void_p),
-                ('auto_scale_b', c_int32)]
+                ('auto_scale_b', c_int32), ('chunk_steps', c_int32)]
 
 
 class SplitPrepareDesc(ctypes.Structure):
@@ -166,7 +166,7 @@ class RedfieldAdjointSplitDesc(ctypes.Structure):
                 ('obs_ops', c_void_p), ('obs_grad', c_void_p),
                 ('grad_R', c_void_p), ('grad_obs', c_void_p),
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
-                ('status', c_void_p)]
+                ('status', c_void_p), ('stage_in', c_void_p)]
 
 
 class RedfieldRK4Desc(ctypes.Structure):
@@ -185,7 +185,7 @@ class RedfieldSplitDesc(ctypes.Structure):
                 ('R', c_void_p), ('rho', c_void_p),
                 ('obs_ops', c_void_p), ('obs_out', c_void_p),
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
-                ('status', c_void_p)]
+                ('status', c_void_p), ('stage_out', c_void_p)]
 
 
 class LindbladStreamDesc(ctypes.Structure):

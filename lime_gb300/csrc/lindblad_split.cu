@@ -917,7 +917,7 @@ extern "C" int lime_lindblad_split_prepare(const LimeLindbladSplitPrepareDesc* d
 
 extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* stream) {
   if (!d) return LIME_ERR_ARG;
-  if (d->n <= 0 || d->batch <= 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (d->n <= 0 || d->batch <= 0 || d->n_steps < 0 || d->n_obs < 0 || d->chunk_steps < 0) return LIME_ERR_ARG;
   if (d->n > split::kN) return LIME_ERR_UNSUPPORTED;
   if (!d->rho || !d->heff || !d->status) return LIME_ERR_ARG;
   if (d->obs_mode < 0 || d->obs_mode > 2) return LIME_ERR_ARG;
@@ -1023,7 +1023,8 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
   LIME_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // bounded launches: about 2^22 instance-steps per launch
   const double per_cta = (double)((d->batch + grid - 1) / grid);
-  int chunk = (int)fmax(1.0, fmin((double)d->n_steps, 4194304.0 / (per_cta * grid)));
+  int chunk = d->chunk_steps > 0 ? d->chunk_steps
+                                 : (int)fmax(1.0, fmin((double)d->n_steps, 4194304.0 / (per_cta * grid)));
   if (a.obs_every > 1) chunk = ((chunk + a.obs_every - 1) / a.obs_every) * a.obs_every;
   for (int s0 = 0; s0 < d->n_steps; s0 += chunk) {
     a.step0 = s0;
@@ -1031,6 +1032,7 @@ extern "C" int lime_lindblad_rk4_split(const LimeLindbladSplitDesc* d, void* str
     kern<<<grid, split::kThreads, smem, st>>>(a);
     LIME_CUDA_TRY(cudaGetLastError());
     count_launch();
+    a.rho = a.rho_out;   // the next launch continues from this one's final state
   }
   return LIME_OK;
 }

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
   T.n_chunks = KC;
   T.row_inv = (k3m ? a.rinv3[p] : a.row_inv) + (size_t)mt * kBM;
   T.inv_sb = (kMode == 2) ? ldexpf(1.f, -*a.sl_exp) : (k3m ? a.inv_sb3[p] : a.inv_sb);
-  T.park_split = kMode == 4;
+  T.park_split = k3m;   // the 3M products cancel: keep their two-sum words
   T.max_wait = a.max_wait;
   T.a_avail = a.a_bytes - (size_t)mt * a.KC * kPiece;
   T.b_avail = a.b_bytes - (size_t)nt * a.KC * kPiece;
@@ -132,7 +132,8 @@ __global__ void __launch_bounds__(sg::kThreads, 1) gemm_kernel(StageArgs a) {
 #pragma unroll 4
         for (int c = 0; c < sg::kEpiCols; ++c) {
           const int jj = nt * kBN + sg::kEpiCols * hh + c;
-          const double v = (double)ft[(sg::kEpiCols * hh + c) * kFStride + r];
+          double v = (double)ft[(sg::kEpiCols * hh + c) * kFStride + r];
+          if (k3m) v += (double)S.lo[(sg::kEpiCols * hh + c) * kBM + r];
           if (k3m) {
             // real product p: column jj is right-hand side jj
             if (jj < a.R) {
@@ -843,6 +844,7 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
   // first B input = rho0
   a.Bn[0] = B[0]; a.Bn[1] = B[1];
   const size_t tot = (size_t)W * Dp;
+  a.ystore = d->stage_out;
   const int ib = (int)((tot / 8 + 255) / 256);
   rsp::init_state_kernel<<<ib < 65535 ? ib : 65535, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->rho), D,
                                                                    d->n_rhs);
@@ -881,6 +883,8 @@ extern "C" int lime_redfield_rk4_split(const LimeRedfieldSplitDesc* d, void* str
       a.stage = s;
       a.Bc[0] = B[2 * cur]; a.Bc[1] = B[2 * cur + 1];
       a.Bn[0] = B[2 * (cur ^ 1)]; a.Bn[1] = B[2 * (cur ^ 1) + 1];
+      if (d->stage_out != nullptr)   // the input of the next stage (stage 3: the new state)
+        a.ystore = d->stage_out + (s < 3 ? (size_t)step * 4 + s + 1 : (size_t)(step + 1) * 4) * tot;
       rsp::gemm_kernel<0><<<MT * NT, sg::kThreads, smem, st>>>(a);
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
@@ -944,6 +948,7 @@ extern "C" size_t lime_redfield_split3_workspace(int32_t n, int32_t n_rhs, int32
 
 extern "C" int lime_redfield_rk4_split3(const LimeRedfieldSplitDesc* d, void* stream) {
   if (!d || d->n <= 0 || d->n_rhs <= 0 || d->n_steps < 0 || d->n_obs < 0) return LIME_ERR_ARG;
+  if (d->stage_out != nullptr) return LIME_ERR_UNSUPPORTED;
   if (!d->R || !d->rho || !d->workspace || !d->status) return LIME_ERR_ARG;
   if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
   if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60) return LIME_ERR_ARG;
@@ -1165,6 +1170,7 @@ extern "C" int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d
   float* Plo = reinterpret_cast<float*>(w); w += L.state;
   float* Acc = reinterpret_cast<float*>(w); w += L.state;
   float* ys = reinterpret_cast<float*>(w); w += (4 * (size_t)S + 1) * L.state;   // [S][4] + after
+  if (d->stage_in != nullptr) ys = const_cast<float*>(d->stage_in);   // the caller's; only read
   float* Lhi = reinterpret_cast<float*>(w); w += L.state;
   float* Llo = reinterpret_cast<float*>(w); w += L.state;
   float* LAcc = reinterpret_cast<float*>(w); w += L.state;
@@ -1222,16 +1228,19 @@ extern "C" int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d
   a.a_bytes = L.apiece; a.b_bytes = L.bpiece; a.st_floats = stf;
   a.Bn[0] = B[0]; a.Bn[1] = B[1];
   a.ystore = ys;
-  const int ib = (int)((stf / 8 + 255) / 256);
-  rsp::init_state_kernel<<<ib < 65535 ? ib : 65535, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->ckpt), D, R);
-  LIME_CUDA_TRY(cudaGetLastError());
-  ++launches;
   const size_t smem = sg::kSmemBytes;
   LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   LIME_CUDA_TRY(cudaFuncSetAttribute(rsp::gemm_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int ib = (int)((stf / 8 + 255) / 256);
+  if (d->stage_in == nullptr) {
+    rsp::init_state_kernel<<<ib < 65535 ? ib : 65535, 256, 0, st>>>(a, reinterpret_cast<const double2*>(d->ckpt), D,
+                                                                     R);
+    LIME_CUDA_TRY(cudaGetLastError());
+    ++launches;
+  }
   int cur = 0;
-  for (int step = 0; step < S; ++step) {
+  for (int step = 0; step < (d->stage_in == nullptr ? S : 0); ++step) {
     for (int s = 0; s < 4; ++s) {
       a.stage = s;
       a.Bc[0] = B[2 * cur]; a.Bc[1] = B[2 * cur + 1];

@@ -389,7 +389,7 @@ def _split_obs(e_ops, n, P, device):
 
 def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: int, e_ops,
                obs_every: int, trace_tol: float, param_batch: int, events=None,
-               ctas_per_sm: int = 0, drive=None, rho_out=None):
+               ctas_per_sm: int = 0, drive=None, rho_out=None, chunk_steps: int = 0):
     """The batched tensor-core kernel (n <= 64, diagonal collapse operators).
     The A operand is split once per generator (``split_operands``); each
     instance takes its state scale from its own rho(0) on the device
@@ -434,6 +434,7 @@ def _run_split(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: in
     if rho_out is not None:
         d.rho_out = rho_out.data_ptr()
     d.ctas_per_sm = ctas_per_sm
+    d.chunk_steps = chunk_steps
     d.dt, d.trace_tol = float(dt), float(trace_tol)
     d.rho = rho.data_ptr()
     d.heff, d.heff_stride = gen.heff.data_ptr(), (0 if gen.heff.shape[0] == 1 else n * n)

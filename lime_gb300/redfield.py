@@ -174,13 +174,24 @@ def _pow2_floor(x: float) -> int:
 SPLIT_PRODUCT = '4m'   # complex product of the tensor-core Redfield RK4 ('3m' or '4m')
 
 
+def stage_buffer_floats(n: int, n_rhs: int, n_steps: int) -> int:
+    """Floats of the stage-input buffer of ``propagate_vec_split(...,
+    stage_out=...)``: [4 n_steps + 1][2 Rp][Dp], Rp = n_rhs rounded up to
+    64, Dp = n^2 rounded up to 128."""
+    Rp = -(-n_rhs // 64) * 64
+    Dp = -(-(n * n) // 128) * 128
+    return (4 * n_steps + 1) * 2 * Rp * Dp
+
+
 def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=None, obs_every=1,
-                        max_retries=3, product=None):
+                        max_retries=3, product=None, stage_out=None):
     """Tensor-core split-precision RK4 (``lime_redfield_rk4_split``) of
     eigenbasis density matrices (B, n, n) under the dense generator.
     ``product``: '4m' (the real block form of the complex product) or '3m'
     (three real products, ``lime_redfield_rk4_split3``); default
-    ``SPLIT_PRODUCT``.
+    ``SPLIT_PRODUCT``.  ``stage_out``: a float32 device tensor of
+    ``stage_buffer_floats(n, B, n_steps)`` elements that receives every
+    stage input (for the adjoint without recomputation; block form only).
 
     Same returns as ``propagate_vec`` without states.  The states are
     scaled to max |rho0| * 1.25 <= 2^13 (a power of two, so the scaling is
@@ -204,6 +215,10 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
     product = SPLIT_PRODUCT if product is None else product
     if product not in ('3m', '4m'):
         raise ValueError("product must be '3m' or '4m'")
+    if stage_out is not None:
+        product = '4m'
+        if stage_out.dtype != torch.float32 or stage_out.numel() < stage_buffer_floats(n, B, n_steps):
+            raise ValueError('stage_out needs stage_buffer_floats(n, n_rhs, n_steps) float32 elements')
     name = 'lime_redfield_rk4_split3' if product == '3m' else 'lime_redfield_rk4_split'
     run = getattr(lib, name)
     wsb = (lib.lime_redfield_split3_workspace if product == '3m' else lib.lime_redfield_split_workspace)(n, B, n_obs)
@@ -224,6 +239,8 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
             d.obs_ops, d.obs_out = E.data_ptr(), obs.data_ptr()
         d.workspace, d.workspace_bytes = aligned, wsb
         d.status = status.data_ptr()
+        if stage_out is not None:
+            d.stage_out = stage_out.data_ptr()
         nat.check(run(d, engine._stream_ptr()), name)
         flags = int(status.item())
         if flags & nat.LIME_FLAG_RANGE and attempt < max_retries:

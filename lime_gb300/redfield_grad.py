@@ -27,7 +27,7 @@ import torch
 
 from . import _native as nat
 from . import engine
-from .redfield import propagate_vec, propagate_vec_split
+from .redfield import propagate_vec, propagate_vec_split, stage_buffer_floats
 
 CDT = torch.complex128
 
@@ -101,22 +101,41 @@ class _Propagate(torch.autograd.Function):
     discrete adjoint (lime_redfield_adjoint_f64) backward."""
 
     @staticmethod
-    def forward(ctx, R, r0, E, dt, n_steps, obs_every, checkpoint, precision):
+    def forward(ctx, R, r0, E, dt, n_steps, obs_every, checkpoint, precision, keep_bytes):
         n = r0.shape[-1]
+        B = r0.shape[0]
         Rg = (R.detach(), n)
         rho = r0.detach().to(CDT).contiguous()
         E = E.detach().to(CDT).contiguous()
+        segs = _segments(n_steps, checkpoint)
+        # split path: the stage inputs of the last segments, as many as fit
+        # keep_bytes, stay in device memory for the backward pass (which
+        # then skips their recomputation)
+        stages = [None] * len(segs)
+        if precision == 'split' and keep_bytes:
+            left = int(keep_bytes)
+            for i in range(len(segs) - 1, -1, -1):
+                need = stage_buffer_floats(n, B, segs[i][1]) * 4
+                if need > left:
+                    break
+                stages[i] = torch.empty(stage_buffer_floats(n, B, segs[i][1]), dtype=torch.float32,
+                                        device=rho.device)
+                left -= need
         ckpts, parts = [], []
-        for s0, m in _segments(n_steps, checkpoint):
+        for (s0, m), sbuf in zip(segs, stages):
             ckpts.append(rho)
             if precision == 'fp64':
                 o, _, rho = propagate_vec(Rg, rho, dt, m, list(E), obs_every=obs_every)
+            elif sbuf is not None:
+                o, _, rho = propagate_vec_split(Rg, rho, dt, m, list(E), obs_every=obs_every, stage_out=sbuf)
             else:
-                o, _, rho = propagate_vec_split(Rg, rho, dt, m, list(E), obs_every=obs_every)
+                # the block form: the backward pass recomputes segments with it
+                o, _, rho = propagate_vec_split(Rg, rho, dt, m, list(E), obs_every=obs_every, product='4m')
             parts.append(o)
         obs = torch.cat(parts, 1) if parts else torch.zeros((rho.shape[0], 0, E.shape[0]), dtype=CDT,
                                                            device=rho.device)
         ctx.save_for_backward(R.detach(), E, *ckpts)
+        ctx.stages = stages
         ctx.cfg = (float(dt), int(n_steps), int(obs_every), int(checkpoint), precision)
         return obs
 
@@ -124,7 +143,8 @@ class _Propagate(torch.autograd.Function):
     def backward(ctx, g):
         R, E, *ckpts = ctx.saved_tensors
         if ctx.cfg[4] == 'split':
-            return _backward_split(R, E, ckpts, g, *ctx.cfg[:4])
+            stages, ctx.stages = ctx.stages, None
+            return _backward_split(R, E, ckpts, g, *ctx.cfg[:4], stages=stages) + (None,)
         lib = nat.require_device()
         dt, n_steps, obs_every, checkpoint = ctx.cfg[:4]
         B, n = ckpts[0].shape[0], ckpts[0].shape[-1]
@@ -151,15 +171,17 @@ class _Propagate(torch.autograd.Function):
             d.workspace, d.workspace_bytes = ws.data_ptr(), wsb
             nat.check(lib.lime_redfield_adjoint_f64(d, engine._stream_ptr()), 'lime_redfield_adjoint_f64')
         g_r0 = lam.transpose(0, 1).reshape(B, n, n)
-        return gR, g_r0, gE, None, None, None, None, None
+        return gR, g_r0, gE, None, None, None, None, None, None
 
 
-def _backward_split(R, E, ckpts, g, dt, n_steps, obs_every, checkpoint, max_retries=3):
+def _backward_split(R, E, ckpts, g, dt, n_steps, obs_every, checkpoint, max_retries=3, stages=None):
     """The backward pass on the tensor cores (lime_redfield_adjoint_split),
     segment by segment from the last; a segment whose adjoint operands left
     their fixed-point range is repeated with a 4x larger margin (a smaller
-    power-of-two scale of the adjoint stage inputs) or, for the stored
-    states, a 4x smaller state scale."""
+    power-of-two scale of the adjoint stage inputs) or, for the recomputed
+    states, a 4x smaller state scale.  ``stages[i]``: segment i's stage
+    inputs kept by the forward pass (its recomputation is skipped), or
+    None."""
     lib = nat.require_device()
     B, n = ckpts[0].shape[0], ckpts[0].shape[-1]
     D = n * n
@@ -174,7 +196,8 @@ def _backward_split(R, E, ckpts, g, dt, n_steps, obs_every, checkpoint, max_retr
     ws = torch.empty(wsb + 1024, dtype=torch.uint8, device=dev)
     aligned = (ws.data_ptr() + 1023) // 1024 * 1024
     status = torch.zeros(1, dtype=torch.int32, device=dev)
-    for (s0, m), ck in reversed(list(zip(segs, ckpts))):
+    stages = stages or [None] * len(segs)
+    for (s0, m), ck, sbuf in reversed(list(zip(segs, ckpts, stages))):
         P = ck.reshape(B, D).contiguous()
         pmax = float(torch.view_as_real(P).abs().max().item())
         sb = int(np.floor(np.log2(8192.0 / (1.25 * pmax)))) if pmax > 0 else 0
@@ -193,21 +216,25 @@ def _backward_split(R, E, ckpts, g, dt, n_steps, obs_every, checkpoint, max_retr
             d.grad_R, d.grad_obs = gR_t.data_ptr(), gE_t.data_ptr()
             d.workspace, d.workspace_bytes = aligned, wsb
             d.status = status.data_ptr()
+            if sbuf is not None:
+                d.stage_in = sbuf.data_ptr()
             nat.check(lib.lime_redfield_adjoint_split(d, engine._stream_ptr()), 'lime_redfield_adjoint_split')
             flags = int(status.item())
             if flags & nat.LIME_FLAG_RANGE and attempt < max_retries:
                 margin += 2
-                sb -= 2
+                if sbuf is None:
+                    sb -= 2
                 continue
             if flags:
                 raise nat.KernelFlagError(flags, 'lime_redfield_adjoint_split')
             break
         lam, gR, gE = lam_t, gR + gR_t, gE + gE_t
+        sbuf = None
     return gR, lam.reshape(B, n, n), gE, None, None, None, None, None
 
 
 def redfield_observables(H, a_ops, spectrum, rho0, e_ops, dt: float, n_steps: int, obs_every: int = 1,
-                         checkpoint: int = 64, precision: str = 'fp64'):
+                         checkpoint: int = 64, precision: str = 'fp64', keep_stages='auto'):
     """<E_o>(t) = Tr(E_o rho(t)) of the Bloch-Redfield evolution of ``rho0``,
     differentiable (torch.autograd) in every tensor input.
 
@@ -220,7 +247,11 @@ def redfield_observables(H, a_ops, spectrum, rho0, e_ops, dt: float, n_steps: in
     obs_every = 1).  ``precision='split'`` runs the forward and the backward
     pass on the tensor cores (lime_redfield_rk4_split,
     lime_redfield_adjoint_split).  ``checkpoint`` must be a multiple of
-    ``obs_every``.
+    ``obs_every``.  ``keep_stages`` (split path): bytes of device memory in
+    which the forward pass keeps the stage inputs of its last checkpoint
+    segments, so that the backward pass recomputes only the others; 'auto'
+    is half the free device memory, 0 recomputes every segment (the
+    gradients are the same either way).
     """
     if precision not in ('fp64', 'split'):
         raise ValueError("precision must be 'fp64' or 'split'")
@@ -252,4 +283,11 @@ def redfield_observables(H, a_ops, spectrum, rho0, e_ops, dt: float, n_steps: in
         else torch.as_tensor(e_ops, device=dev)
     r0e = Vc.mH @ r0 @ Vc
     Ee = Vc.mH @ Es.to(CDT) @ Vc
-    return _Propagate.apply(R, r0e, Ee, float(dt), int(n_steps), int(obs_every), int(checkpoint), precision)
+    keep = 0
+    if precision == 'split':
+        if keep_stages == 'auto':
+            keep = torch.cuda.mem_get_info(dev)[0] // 2 if torch.is_grad_enabled() else 0
+        else:
+            keep = int(keep_stages)
+    return _Propagate.apply(R, r0e, Ee, float(dt), int(n_steps), int(obs_every), int(checkpoint), precision,
+                            keep)

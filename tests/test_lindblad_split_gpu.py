@@ -176,3 +176,36 @@ def test_prepared_operand_matches_in_kernel_split():
         assert int(st.item()) == 0
         outs.append((obs, out))
     assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+
+
+@pytest.mark.parametrize('chunk,obs_every', [(7, 3), (40, 40), (1, 1)])
+def test_multi_launch_continues_the_state(chunk, obs_every):
+    """A call split into several launches (chunk_steps) continues every
+    launch from the state the previous one wrote to rho_out: observables
+    and final states as in one launch (up to the per-launch state scale)
+    and within the bar of the FP64 path.  (A long call of the full ensemble
+    is split this way: 4096 realisations x 4000 steps run as 4 launches.)"""
+    from lime_gb300 import engine
+    n, batch, steps = 24, 6, 120
+    w, c_ops = _ensemble(n, batch, steps)
+    gen = engine.LindbladGenerator.build(w['H'], c_ops)
+    E = chains.population_ops(n)
+    o64, _, r64 = engine.propagate(gen, w['rho0'], w['dt'], steps, E, obs_every=obs_every)
+    rho = torch.as_tensor(np.stack([w['rho0']] * batch if np.ndim(w['rho0']) == 2 else w['rho0']),
+                          device='cuda').contiguous()
+    outs = []
+    for ck in (0, chunk):
+        out = torch.empty_like(rho)
+        o, _, status = engine._run_split(gen, rho, w['dt'], steps, E, obs_every, 1e-5, batch, rho_out=out,
+                                         chunk_steps=ck)
+        torch.cuda.synchronize()
+        assert int(status.item()) == 0
+        outs.append((o, out))
+    (o1, r1), (oc, rc) = outs
+    assert (oc - o1).abs().max().item() < 1e-7
+    assert (rc - r1).abs().max().item() < 1e-7
+    assert (oc - o64).abs().max().item() < POP_TOL
+    assert (rc - r64).abs().max().item() < POP_TOL
+    # the input is not modified
+    assert torch.equal(rho, torch.as_tensor(np.stack([w['rho0']] * batch if np.ndim(w['rho0']) == 2
+                                                     else w['rho0']), device='cuda'))

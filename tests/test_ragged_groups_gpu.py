@@ -41,9 +41,11 @@ def _run(sched, steps=24, sizes=SIZES, seed=3, prec='split'):
 
 
 def _same(a, b):
+    """(obs, states, rho) lists equal bit for bit (states None on both)."""
     for x, y in zip(a, b):
+        assert len(x) == len(y)
         for u, v in zip(x, y):
-            assert torch.equal(u, v)
+            assert (u is None and v is None) or torch.equal(u, v)
 
 
 def test_grouped_launch_matches_streams_bitwise_and_fp64():

@@ -153,7 +153,7 @@ def test_redfield_split_adjoint_raw_outputs():
         out = {}
         for prec in ('fp64', 'split'):
             leaves = [x.clone().requires_grad_(True) for x in (R.R, r0, E)]
-            obs = _Propagate.apply(*leaves, 0.05, steps, 1, ck, prec)
+            obs = _Propagate.apply(*leaves, 0.05, steps, 1, ck, prec, 0)
             g = torch.tensor(np.random.default_rng(1).normal(size=tuple(obs.shape)), device='cuda').to(CDT)
             (obs.conj() * g).real.sum().backward()
             out[prec] = [x.grad for x in leaves]
@@ -190,3 +190,29 @@ def test_redfield_split_adjoint_larger_block():
     _, gsp = _grads(lambda *p: _loss_lib(m, *p, weights, steps, obs_every, ckpt, 'split'), params)
     for a, b in zip(gsp, g64):
         assert (a - b).abs().max().item() <= SPLIT_PARAM_TOL * max(b.abs().max().item(), 1e-300)
+
+
+def test_redfield_split_kept_stage_inputs_give_the_same_gradients():
+    """Stage inputs kept from the forward pass (no recomputation) against
+    recomputed ones: bitwise the same gradients, with every segment kept and
+    with only the last one kept."""
+    n, steps, obs_every, ckpt = 7, 45, 1, 20
+    m = _model(n, 14)
+    weights = torch.tensor(m['rng'].normal(size=(2, steps // obs_every, n)), device='cuda')
+    params = [m['eps'], m['J'], m['s'], m['lam']]
+
+    def grads(keep):
+        from lime_gb300.redfield_grad import redfield_observables, ohmic_spectrum
+        ps = [p.clone().requires_grad_(True) for p in params]
+        H, a_ops = _inputs(m, *ps)
+        obs = redfield_observables(H, a_ops, ohmic_spectrum(ps[3], 0.1, 0.025), m['rho0'], m['E'], 0.05, steps,
+                                   obs_every=obs_every, checkpoint=ckpt, precision='split', keep_stages=keep)
+        (obs.real * weights).sum().backward()
+        return [p.grad for p in ps]
+
+    from lime_gb300.redfield import stage_buffer_floats
+    g0 = grads(0)
+    last = stage_buffer_floats(n, 2, steps - 2 * ckpt) * 4
+    for keep in ('auto', last):
+        for a, b in zip(grads(keep), g0):
+            assert torch.equal(a, b)

@@ -1,9 +1,16 @@
 """The 3M form of the tensor-core Redfield RK4 (lime_redfield_rk4_split3:
 three real products instead of the four of the block form) against the
-FP64 GPU path: observables and final states within 1e-6 of the FP64
-results relative to their largest magnitude, Hermitian and non-Hermitian
-right-hand sides, right-hand-side counts on both sides of a 128-column
-tile."""
+FP64 GPU path, Hermitian and non-Hermitian right-hand sides,
+right-hand-side counts on both sides of a 128-column tile.
+
+Bars: observables (populations and a coherence, all of magnitude <= 1)
+within 1e-6 absolute of FP64, final states within 1e-6 relative to their
+largest element, and within 4x the block form's error.  The observables
+are read from the state's B operand (10-bit fixed point + fp16 residual,
+about 2^-22 of the largest element per entry), which bounds both forms'
+readout error to a few 1e-7 on these small systems (the block form 2.4e-7,
+the 3M form 5.8e-7 on the 8-site chain, constant over 1..800 steps); the
+propagated states themselves differ from FP64 by ~2e-8."""
 import numpy as np
 import pytest
 import torch
@@ -54,10 +61,12 @@ def test_split3_matches_fp64(n, n_rhs, steps, nh):
     o3, _, p3 = propagate_vec_split(Rg, r0, 0.05, steps, E, product='3m')
     o4, _, p4 = propagate_vec_split(Rg, r0, 0.05, steps, E, product='4m')
     assert o3.shape == o64.shape
-    assert rel(o3.cpu(), o64.cpu()) < TOL
+    e3, e4 = (o3 - o64).abs().max().item(), (o4 - o64).abs().max().item()
+    assert e3 < TOL, (e3, e4)
     assert rel(p3.cpu(), p64.cpu()) < TOL
     # and about as close as the block form
-    assert rel(o3.cpu(), o64.cpu()) < 10 * max(rel(o4.cpu(), o64.cpu()), 1e-9)
+    assert e3 < 4 * max(e4, 1e-9), (e3, e4)
+    assert rel(p3.cpu(), p64.cpu()) < 4 * max(rel(p4.cpu(), p64.cpu()), 1e-10)
 
 
 def test_split3_obs_every_and_no_observables():
@@ -68,7 +77,7 @@ def test_split3_obs_every_and_no_observables():
     o64, _, _ = propagate_vec(Rg, r0, 0.05, 30, E)
     o3, _, _ = propagate_vec_split(Rg, r0, 0.05, 30, E, obs_every=3, product='3m')
     assert o3.shape[1] == 10
-    assert rel(o3.cpu(), o64[:, 2::3].cpu()) < TOL
+    assert (o3 - o64[:, 2::3]).abs().max().item() < TOL
     _, _, p3 = propagate_vec_split(Rg, r0, 0.05, 30, None, product='3m')
     _, _, p64 = propagate_vec(Rg, r0, 0.05, 30, None)
     assert rel(p3.cpu(), p64.cpu()) < TOL
