@@ -479,7 +479,7 @@ def redfield_adjoint_leg(torch, dev, n=96, n_rhs=512, steps=128, checkpoint=64, 
     E = torch.as_tensor(np.stack(chains.population_ops(n)), device=dev)
     wts = torch.tensor(np.random.default_rng(5).normal(size=(n_rhs, steps, n)), device=dev)
 
-    def run(grad):
+    def run(grad, keep=0):
         eps = eps0.clone().requires_grad_(grad)
         J = torch.tensor(-0.1, dtype=torch.float64, device=dev, requires_grad=grad)
         s = torch.ones(n, dtype=torch.float64, device=dev, requires_grad=grad)
@@ -487,7 +487,7 @@ def redfield_adjoint_leg(torch, dev, n=96, n_rhs=512, steps=128, checkpoint=64, 
         H = torch.diag(eps) + J * (off + off.T)
         a_ops = s[:, None, None] * torch.diag_embed(proj)
         obs = redfield_observables(H, a_ops, ohmic_spectrum(lam, 0.1, 0.025), rho0, E, dt, steps,
-                                   checkpoint=checkpoint, precision='split')
+                                   checkpoint=checkpoint, precision='split', keep_stages=keep)
         return (obs.real * wts).sum(), (eps, J, s, lam)
 
     def timed(fn):
@@ -502,16 +502,23 @@ def redfield_adjoint_leg(torch, dev, n=96, n_rhs=512, steps=128, checkpoint=64, 
     with torch.no_grad():
         run(False)                      # warm
         _, tf = timed(lambda: run(False))
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    torch.cuda.synchronize()
-    ev[0].record()
-    loss, params = run(True)
-    ev[1].record()
-    loss.backward()
-    ev[2].record()
-    torch.cuda.synchronize()
-    tfg = ev[0].elapsed_time(ev[1]) / 1e3
-    tb = ev[1].elapsed_time(ev[2]) / 1e3
+    def grad_run(keep):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        ev[0].record()
+        loss, params = run(True, keep)
+        ev[1].record()
+        loss.backward()
+        ev[2].record()
+        torch.cuda.synchronize()
+        return ev[0].elapsed_time(ev[1]) / 1e3, ev[1].elapsed_time(ev[2]) / 1e3, params
+
+    tfg, tb, params = grad_run(0)
+    free = torch.cuda.mem_get_info(dev)[0] // 2
+    tfk, tbk, pk = grad_run(free)
+    same = all(torch.equal(a.grad, b.grad) for a, b in zip(params, pk))
+    from lime_gb300.redfield import stage_buffer_floats
+    seg_gb = stage_buffer_floats(n, n_rhs, checkpoint) * 4 / 1e9
     return {'workload': 'Redfield N=%d (Liouville dim %d), %d right-hand sides, weighted populations; grads '
                         'w.r.t. %d site energies, J, %d bath coupling strengths and the reorganisation energy; '
                         'checkpoint every %d steps; %d-step sample of the 2000-step workload'
@@ -519,6 +526,10 @@ def redfield_adjoint_leg(torch, dev, n=96, n_rhs=512, steps=128, checkpoint=64, 
             'path': 'split forward and backward (lime_redfield_rk4_split, lime_redfield_adjoint_split)',
             'forward_s': tf, 'forward_with_checkpoints_s': tfg, 'adjoint_s': tb,
             'adjoint_over_forward': tb / tf,
+            'kept': {'keep_bytes': int(free), 'segment_gb': seg_gb,
+                     'segments_kept': int(min(-(-steps // checkpoint), free // max(1, int(seg_gb * 1e9)))),
+                     'forward_keeping_s': tfk, 'adjoint_s': tbk, 'adjoint_over_forward': tbk / tf,
+                     'gradients_bitwise_equal_to_recompute': bool(same)},
             'grad_norms': [float(p.grad.abs().max().item()) for p in params]}
 
 
@@ -567,6 +578,8 @@ def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k
     issued = {'4m': 5 * stage_flop, '3m': 5 * 0.75 * stage_flop}
     pk = peaks.get('bf16_tflops_sustained') or 1700.0
     prod = rfm.SPLIT_PRODUCT
+    if prod == 'auto':
+        prod = '3m' if n * n >= rfm.SPLIT_3M_MIN_DIM else '4m'
     split_rate = n_rhs / per_step[prod]
     fp64_rate = n_rhs * k64 / t64
 
@@ -885,7 +898,8 @@ def e2e_leg(wl, K, path, dev):
     pops = Populations(N_SITES)
     nout = max(1, K // 100)
     sol = Lindblad_solver(H, c_ops=[SiteDephasing(g)], precision=path)
-    sol.evolve(rho0, dt=DT, Nt=2, e_ops=pops, store_states=False)  # warm
+    for _ in range(2):   # warm: the same call, so the timed one reuses cached pinned result blocks
+        sol.evolve(rho0, dt=DT, Nt=K, e_ops=pops, nout=nout, store_states=False)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     res = sol.evolve(rho0, dt=DT, Nt=K, e_ops=pops, nout=nout, store_states=False)

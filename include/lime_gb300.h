@@ -391,6 +391,30 @@ size_t lime_redfield_adjoint_split_workspace(int32_t n, int32_t n_rhs, int32_t s
 int lime_redfield_adjoint_split(const LimeRedfieldAdjointSplitDesc* d, void* stream);
 
 /* ------------------------------------------------------------------ */
+/* Green's-function route and basis changes (FP64)                      */
+/* ------------------------------------------------------------------ */
+
+/* Strided batched complex128 GEMM
+ *     C[z][i][j] = sum_k op(A)[z][i][k] * scale[z][k] * op(B)[z][k][j]
+ * for z < batch, i < M, j < N, k < K; op conjugates when conj_a / conj_b
+ * is 1.  Strides are in complex elements (row, column, batch; 0
+ * broadcasts); scale is optional (NULL: 1).  Replaces the propagator and
+ * Green's-function contractions of Redfield_solver (lime/oqs.py:169-366:
+ * U(t_z) = U1 diag(exp(w t_z)) U1^-1 as one call with scale = exp(w t_z),
+ * expect, correlation_2op_1t, correlation_4op_3t) and the eigenbasis
+ * transforms V^dag X V (lime/phys.py:706-718, lime/oqs.py:430-440). */
+typedef struct {
+  int32_t M, N, K, batch;
+  int32_t conj_a, conj_b;
+  const double* A;        int64_t a_rs, a_cs, a_bs;
+  const double* B;        int64_t b_rs, b_cs, b_bs;
+  const double* scale;    int64_t s_ks, s_bs;
+  double* C;              int64_t c_rs, c_cs, c_bs;
+} LimeZgemmDesc;
+
+int lime_zgemm_strided_f64(const LimeZgemmDesc* d, void* stream);
+
+/* ------------------------------------------------------------------ */
 /* General Lindblad RK4 on the tensor cores (split precision)           */
 /* ------------------------------------------------------------------ */
 

@@ -188,6 +188,15 @@ class RedfieldSplitDesc(ctypes.Structure):
                 ('status', c_void_p), ('stage_out', c_void_p)]
 
 
+class ZgemmDesc(ctypes.Structure):
+    _fields_ = [('M', c_int32), ('N', c_int32), ('K', c_int32), ('batch', c_int32),
+                ('conj_a', c_int32), ('conj_b', c_int32),
+                ('A', c_void_p), ('a_rs', c_int64), ('a_cs', c_int64), ('a_bs', c_int64),
+                ('B', c_void_p), ('b_rs', c_int64), ('b_cs', c_int64), ('b_bs', c_int64),
+                ('scale', c_void_p), ('s_ks', c_int64), ('s_bs', c_int64),
+                ('C', c_void_p), ('c_rs', c_int64), ('c_cs', c_int64), ('c_bs', c_int64)]
+
+
 class LindbladStreamDesc(ctypes.Structure):
     _fields_ = [('n', c_int32), ('batch', c_int32), ('param_batch', c_int32), ('n_ops', c_int32),
                 ('n_steps', c_int32), ('n_obs', c_int32), ('obs_every', c_int32),
@@ -244,6 +253,7 @@ SIGNATURES = [
     ('lime_redfield_split_workspace', c_size_t, [c_int32, c_int32, c_int32]),
     ('lime_redfield_rk4_split', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_redfield_split3_workspace', c_size_t, [c_int32, c_int32, c_int32]),
+    ('lime_zgemm_strided_f64', c_int32, [ctypes.POINTER(ZgemmDesc), c_void_p]),
     ('lime_redfield_rk4_split3', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_lindblad_stream_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_stream', c_int32, [ctypes.POINTER(LindbladStreamDesc), c_void_p]),

@@ -442,41 +442,58 @@ __global__ void __launch_bounds__(kThreads) lindblad_adjoint_f64_kernel(AdjArgs 
   }
 }
 
-// Heff = H - (i/2) sum_k L_k^dag L_k ;  M = sum_k l_k l_k^dag.  When every
-// diagonal operator has at most one nonzero entry (site dephasing), the
-// off-diagonal terms l_k[i] conj(l_k[j]) are exact zeros and are not summed.
+// Heff = H - (i/2) sum_k L_k^dag L_k ;  M = sum_k l_k l_k^dag, one CTA per
+// generator.  The dense part sum_k L_k^dag L_k arrives in heff (a strided
+// batched GEMM run before this kernel) or is absent (k_dense = 0).  For the
+// diagonal operators the diagonal sums dg[i] = sum_k |l_k[i]|^2 (which are
+// both the diagonal of sum_k L_k^dag L_k and of M) are formed once per
+// generator in shared memory, k in order; when every diagonal operator has
+// at most one nonzero entry (site dephasing) the off-diagonal terms
+// l_k[i] conj(l_k[j]) of M are exact zeros and are not summed.
 __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
+  extern __shared__ double dg[];    // [n]
   const int b = blockIdx.x;
   const int n = d.n;
-  const int64_t nn = (int64_t)n * n;
+  const int nn = n * n;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const double2* H = reinterpret_cast<const double2*>(d.h) + b * d.h_stride;
-  const double2* Ld = d.l_dense ? reinterpret_cast<const double2*>(d.l_dense) + b * d.l_dense_stride : nullptr;
   const double2* lg = d.l_diag ? reinterpret_cast<const double2*>(d.l_diag) + b * d.l_diag_stride : nullptr;
-  double2* heff = reinterpret_cast<double2*>(d.heff) + b * nn;
-  double2* M = reinterpret_cast<double2*>(d.m) + b * nn;
+  double2* heff = reinterpret_cast<double2*>(d.heff) + (int64_t)b * nn;
+  double2* M = reinterpret_cast<double2*>(d.m) + (int64_t)b * nn;
   __shared__ int spread;   // some l_k has two or more nonzero entries
-  if (threadIdx.x == 0) spread = 0;
-  __syncthreads();
-  for (int k = threadIdx.x; k < d.k_diag; k += kThreads) {
-    const double2* l = lg + (int64_t)k * n;
-    int nz = 0;
-    for (int q = 0; q < n; ++q) nz += (l[q].x != 0.0 || l[q].y != 0.0) ? 1 : 0;
-    if (nz > 1) atomicOr(&spread, 1);
+  if (t == 0) spread = 0;
+  for (int i = t; i < n; i += kThreads) {
+    double s = 0.0;
+    for (int k = 0; k < d.k_diag; ++k) {
+      const double2 v = lg[(int64_t)k * n + i];
+      s += v.x * v.x + v.y * v.y;
+    }
+    dg[i] = s;
   }
   __syncthreads();
-  for (int64_t e = threadIdx.x; e < nn; e += kThreads) {
-    const int i = (int)(e / n), j = (int)(e % n);
-    double2 g = cz();  // (sum_k L_k^dag L_k)_ij
-    for (int k = 0; k < d.k_dense; ++k) {
-      const double2* L = Ld + k * nn;
-      for (int q = 0; q < n; ++q) cfma(g, cconj(L[(int64_t)q * n + i]), L[(int64_t)q * n + j]);
+  // one warp per operator counts its nonzero entries
+  for (int k = warp; k < d.k_diag; k += kThreads / 32) {
+    int cnt = 0;
+    for (int i0 = 0; i0 < n; i0 += 32) {   // every lane takes part in each ballot
+      const int i = i0 + lane;
+      const double2 v = i < n ? lg[(int64_t)k * n + i] : cz();
+      cnt += __popc(__ballot_sync(0xffffffffu, v.x != 0.0 || v.y != 0.0));
     }
+    if (lane == 0 && cnt > 1) atomicOr(&spread, 1);
+  }
+  __syncthreads();
+  for (int e = t; e < nn; e += kThreads) {
+    const int i = e / n, j = e - i * n;
+    double2 g = d.k_dense > 0 ? heff[e] : cz();   // (sum_k L_k^dag L_k)_ij of the dense operators
     double2 mm = cz();
-    const int k_m = (spread || i == j) ? d.k_diag : 0;
-    for (int k = 0; k < k_m; ++k) {
-      const double2* l = lg + (int64_t)k * n;
-      cfma(mm, l[i], cconj(l[j]));
-      if (i == j) g = cadd(g, make_double2(l[i].x * l[i].x + l[i].y * l[i].y, 0.0));
+    if (i == j) {
+      g.x += dg[i];
+      mm.x = dg[i];
+    } else if (spread) {
+      for (int k = 0; k < d.k_diag; ++k) {
+        const double2* l = lg + (int64_t)k * n;
+        cfma(mm, l[i], cconj(l[j]));
+      }
     }
     // H - (i/2) g  =  (H.re + g.im/2, H.im - g.re/2)
     const double2 h = H[e];
@@ -495,7 +512,22 @@ extern "C" int lime_lindblad_prepare_f64(const LimePrepareDesc* d, void* stream)
   if (!d->h || !d->heff || !d->m) return LIME_ERR_ARG;
   if ((d->k_dense > 0 && !d->l_dense) || (d->k_diag > 0 && !d->l_diag)) return LIME_ERR_ARG;
   if (d->h_stride < 0 || d->l_dense_stride < 0 || d->l_diag_stride < 0) return LIME_ERR_ARG;
-  f64::prepare_kernel<<<d->batch, f64::kThreads, 0, (cudaStream_t)stream>>>(*d);
+  if ((size_t)d->n * sizeof(double) > 48 * 1024) return LIME_ERR_UNSUPPORTED;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (d->k_dense > 0) {
+    // heff[b] = sum_k L_k^dag L_k = [L_1; ..; L_K]^dag [L_1; ..; L_K] (K n x n
+    // stacked), one strided batched FP64 GEMM over the generators
+    LimeZgemmDesc g{};
+    const int64_t n = d->n;
+    g.M = d->n; g.N = d->n; g.K = (int32_t)(d->k_dense * n); g.batch = d->batch;
+    g.conj_a = 1;
+    g.A = d->l_dense; g.a_rs = 1; g.a_cs = n; g.a_bs = d->l_dense_stride;
+    g.B = d->l_dense; g.b_rs = n; g.b_cs = 1; g.b_bs = d->l_dense_stride;
+    g.C = d->heff; g.c_rs = n; g.c_cs = 1; g.c_bs = n * n;
+    const int rc = lime_zgemm_strided_f64(&g, stream);
+    if (rc != LIME_OK) return rc;
+  }
+  f64::prepare_kernel<<<d->batch, f64::kThreads, (size_t)d->n * sizeof(double), st>>>(*d);
   LIME_CUDA_TRY(cudaGetLastError());
   count_launch();
   return LIME_OK;
