@@ -414,6 +414,27 @@ typedef struct {
 
 int lime_zgemm_strided_f64(const LimeZgemmDesc* d, void* stream);
 
+/* Batched complex128 discrete Fourier transform along one axis:
+ *     Y[b][k] = sum_j x[b][j] exp(-+ 2 pi i j k / n)    (- forward, + inverse;
+ *                                                       no 1/n)
+ * written to position (k + n/2) % n when shift = 1 (numpy's fftshift) and
+ * multiplied there by post[position] when post is not NULL.  With post =
+ * dx exp(-i w x0) this is lime's fft (lime/fft.py:9-56).  Strides in
+ * complex elements (along the transform, between transforms).  Power-of-two
+ * n <= 8192 need no workspace; other n <= 4096 take
+ * lime_fft_f64_workspace(n, batch) bytes (16-byte aligned);
+ * LIME_ERR_UNSUPPORTED above. */
+typedef struct {
+  int32_t n, batch, inverse, shift;
+  const double* x;        int64_t x_s, x_bs;
+  double* y;              int64_t y_s, y_bs;
+  const double* post;
+  void* workspace;        size_t workspace_bytes;
+} LimeFftDesc;
+
+size_t lime_fft_f64_workspace(int32_t n, int32_t batch);
+int lime_fft_f64(const LimeFftDesc* d, void* stream);
+
 /* ------------------------------------------------------------------ */
 /* General Lindblad RK4 on the tensor cores (split precision)           */
 /* ------------------------------------------------------------------ */

@@ -197,6 +197,14 @@ class ZgemmDesc(ctypes.Structure):
                 ('C', c_void_p), ('c_rs', c_int64), ('c_cs', c_int64), ('c_bs', c_int64)]
 
 
+class FftDesc(ctypes.Structure):
+    _fields_ = [('n', c_int32), ('batch', c_int32), ('inverse', c_int32), ('shift', c_int32),
+                ('x', c_void_p), ('x_s', c_int64), ('x_bs', c_int64),
+                ('y', c_void_p), ('y_s', c_int64), ('y_bs', c_int64),
+                ('post', c_void_p),
+                ('workspace', c_void_p), ('workspace_bytes', c_size_t)]
+
+
 class LindbladStreamDesc(ctypes.Structure):
     _fields_ = [('n', c_int32), ('batch', c_int32), ('param_batch', c_int32), ('n_ops', c_int32),
                 ('n_steps', c_int32), ('n_obs', c_int32), ('obs_every', c_int32),
@@ -254,6 +262,8 @@ SIGNATURES = [
     ('lime_redfield_rk4_split', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_redfield_split3_workspace', c_size_t, [c_int32, c_int32, c_int32]),
     ('lime_zgemm_strided_f64', c_int32, [ctypes.POINTER(ZgemmDesc), c_void_p]),
+    ('lime_fft_f64_workspace', c_size_t, [c_int32, c_int32]),
+    ('lime_fft_f64', c_int32, [ctypes.POINTER(FftDesc), c_void_p]),
     ('lime_redfield_rk4_split3', c_int32, [ctypes.POINTER(RedfieldSplitDesc), c_void_p]),
     ('lime_lindblad_stream_workspace', c_size_t, [c_int32, c_int32, c_int32, c_int32]),
     ('lime_lindblad_rk4_stream', c_int32, [ctypes.POINTER(LindbladStreamDesc), c_void_p]),
