@@ -480,6 +480,10 @@ typedef struct {
   /* a diagonal M (real M_ii, [P|1][n], stride n or 0) instead of m: the
    * jump term then touches only the diagonal (pure dephasing) */
   const double* m_diag;   int64_t m_diag_stride;
+  /* 1: obs_ops holds only the diagonals of diagonal observables,
+   * [P|1][n_obs][n] complex128 (obs_stride n_obs n or 0), and
+   * Tr(E rho) = sum_x E_xx rho_xx reads n state elements */
+  int32_t obs_diag;
 } LimeLindbladStreamDesc;
 
 size_t lime_lindblad_stream_workspace(int32_t n, int32_t batch, int32_t n_generators, int32_t n_ops);

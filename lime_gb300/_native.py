@@ -219,7 +219,7 @@ class LindbladStreamDesc(ctypes.Structure):
                 ('workspace', c_void_p), ('workspace_bytes', c_size_t),
                 ('status', c_void_p),
                 ('n_drive', c_int32), ('drive_ops', c_void_p), ('drive_coef', c_void_p),
-                ('m_diag', c_void_p), ('m_diag_stride', c_int64)]
+                ('m_diag', c_void_p), ('m_diag_stride', c_int64), ('obs_diag', c_int32)]
 
 
 class AdjointStreamDesc(ctypes.Structure):

@@ -478,16 +478,18 @@ __global__ void init_kernel(Args a, const double2* rho, int batch) {
   if (range) atomicOr(a.status, LIME_FLAG_RANGE);
 }
 
-// obs[b][slot][o] = Tr(E_o rho_b) = sum_xy E_o[x][y] rho[y][x], fp64 from hi + lo
+// obs[b][slot][o] = Tr(E_o rho_b) = sum_xy E_o[x][y] rho[y][x], fp64 from hi + lo;
+// diag: E holds only the diagonals E_o[x][x] ([P|1][n_obs][n]), n terms
 __global__ void observe_kernel(Args a, const double2* E, int64_t e_stride, int n_obs, double2* out, int n_slots,
-                               int slot) {
+                               int slot, int diag) {
   const int b = blockIdx.x / n_obs, o = blockIdx.x % n_obs;
-  const double2* Eo = E + (e_stride ? (int64_t)(b % a.P) * e_stride : 0) + (int64_t)o * a.n * a.n;
+  const int per = diag ? a.n : a.n * a.n;
+  const double2* Eo = E + (e_stride ? (int64_t)(b % a.P) * e_stride : 0) + (int64_t)o * per;
   const size_t base = (size_t)b * inst_floats(a);
   double sr = 0.0, si = 0.0;
-  for (int q = threadIdx.x; q < a.n * a.n; q += blockDim.x) {
-    const int x = q / a.n, y = q - x * a.n;
-    const double2 ev = Eo[(size_t)x * a.n + y];
+  for (int q = threadIdx.x; q < per; q += blockDim.x) {
+    const int x = diag ? q : q / a.n, y = diag ? q : q - x * a.n;
+    const double2 ev = Eo[q];
     // a zero entry adds exactly zero (projectors and dipoles are sparse);
     // non-finite states are flagged by the stage kernels
     if (ev.x == 0.0 && ev.y == 0.0) continue;
@@ -835,7 +837,7 @@ int lsm_prepare(const LimeLindbladStreamDesc* d, LsmRun& r, cudaStream_t st, int
   if (d->n_ops > 0 && !d->l_ops) return LIME_ERR_ARG;
   if (d->n_obs > 0 && (!d->obs_ops || !d->obs_out)) return LIME_ERR_ARG;
   if (d->heff_stride < 0 || d->l_stride < 0 || d->m_stride < 0 || d->obs_stride < 0) return LIME_ERR_ARG;
-  if (d->m_diag_stride < 0) return LIME_ERR_ARG;
+  if (d->m_diag_stride < 0 || (d->obs_diag & ~1)) return LIME_ERR_ARG;
   if (d->scale_b_log2 < -60 || d->scale_b_log2 > 60 || d->scale_y_log2 < -60 || d->scale_y_log2 > 60)
     return LIME_ERR_ARG;
   if (d->n > 4096 || d->n_ops > 64) return LIME_ERR_UNSUPPORTED;
@@ -923,7 +925,8 @@ int lsm_observe(const LimeLindbladStreamDesc* d, LsmRun& r, int step, cudaStream
     lsm::observe_kernel<<<r.B * d->n_obs, 128, 0, st>>>(r.a, reinterpret_cast<const double2*>(d->obs_ops),
                                                         d->obs_stride, d->n_obs,
                                                         reinterpret_cast<double2*>(d->obs_out),
-                                                        d->n_steps / obs_every, (step + 1) / obs_every - 1);
+                                                        d->n_steps / obs_every, (step + 1) / obs_every - 1,
+                                                        d->obs_diag);
     LIME_CUDA_TRY(cudaGetLastError());
     ++launches;
   }

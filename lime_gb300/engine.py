@@ -340,6 +340,16 @@ def split_operands(gen: LindbladGenerator) -> dict:
     return c
 
 
+def _is_diag_host(a) -> bool:
+    """A host operator (or a stack of them) with no nonzero off-diagonal entry."""
+    a = np.asarray(a)
+    if a.ndim < 2 or a.shape[-1] != a.shape[-2]:
+        return False
+    n = a.shape[-1]
+    m = a.reshape(-1, n, n)
+    return not np.any(m[:, ~np.eye(n, dtype=bool)])
+
+
 def _host_array(a):
     """NumPy view of a host operand, or None for a device tensor."""
     if isinstance(a, torch.Tensor):
@@ -487,13 +497,24 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     K = gen.k_dense
     E = None
     n_obs = 0
+    obs_diag = False
     if e_ops:
+        # diagonal observables (populations) go in as their diagonals: the
+        # readout then touches n state elements instead of n^2; decided on
+        # the host for host operators
+        host = [_host_array(e) for e in e_ops]
+        obs_diag = all(h is not None and _is_diag_host(h) for h in host)
         Es = [as_device(e, dev) for e in e_ops]
         if any(e.dim() == 3 for e in Es):
             E = torch.stack([e.expand(gen.P, n, n) if e.dim() == 2 else e for e in Es], 1).contiguous()
         else:
             E = torch.stack(Es, 0).unsqueeze(0).contiguous()
         n_obs = E.shape[1]
+        if not obs_diag and any(h is None for h in host):
+            # device operators: one check per call
+            obs_diag = bool(is_diagonal(E.reshape(-1, n, n)))
+        if obs_diag:
+            E = torch.diagonal(E, dim1=-2, dim2=-1).contiguous()
     n_slots = n_steps // obs_every
     obs_out = torch.zeros((B, max(n_slots, 1), max(n_obs, 1)), dtype=CDT, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
@@ -531,8 +552,9 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
         if K:
             d.l_ops, d.l_stride = gen.l_dense.data_ptr(), (0 if l_shared else K * n * n)
         if E is not None:
-            d.obs_ops, d.obs_stride = E.data_ptr(), (0 if E.shape[0] == 1 else n_obs * n * n)
+            d.obs_ops, d.obs_stride = E.data_ptr(), (0 if E.shape[0] == 1 else E[0].numel())
             d.obs_out = obs_out.data_ptr()
+            d.obs_diag = int(obs_diag)
         d.workspace, d.workspace_bytes = aligned, wsb
         d.status = status.data_ptr()
         if drive is not None:
