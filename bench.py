@@ -579,7 +579,7 @@ def redfield_leg(torch, dev, peaks, n=96, n_rhs=512, dt=0.05, k_split=(4, 12), k
     pk = peaks.get('bf16_tflops_sustained') or 1700.0
     prod = rfm.SPLIT_PRODUCT
     if prod == 'auto':
-        prod = '3m' if n * n >= rfm.SPLIT_3M_MIN_DIM else '4m'
+        prod = rfm.split_product(n, n_rhs, dev)
     split_rate = n_rhs / per_step[prod]
     fp64_rate = n_rhs * k64 / t64
 

@@ -173,13 +173,77 @@ def _pow2_floor(x: float) -> int:
     return int(np.floor(np.log2(x)))
 
 
-# complex product of the tensor-core Redfield RK4: '3m' (three real
-# products per stage, 21 % faster at Liouville dimension 9216, population
-# error 6.4e-8 vs FP64 over 2000 steps) from this Liouville dimension up,
-# the block form '4m' below it (small systems, where the run time is
-# negligible and the block form's observable readout is ~2x closer)
+# complex product of the tensor-core Redfield RK4: the block form '4m'
+# (one launch of 2 Dp / 64-chunk tiles over [Yr | Yi]) or '3m' (three real
+# products: 3/4 of the tensor work in 1.5x as many tiles of half the K, plus
+# an elementwise stage pass).  'auto': the autotuner's cached choice for the
+# shape, else the wave-quantised cost model of split_product(); 3M only from
+# Liouville dimension SPLIT_3M_MIN_DIM up (below it the run time is
+# negligible and the block form's observable readout is ~2x closer).
 SPLIT_3M_MIN_DIM = 1024
 SPLIT_PRODUCT = 'auto'
+
+
+def split_cost(n: int, n_rhs: int, sms: int):
+    """Model of one stage's streaming-GEMM time in chunk-iterations of the
+    busiest CTA, (block form, 3M): waves of tiles x K chunks per tile, the 3M
+    form with 8 % for its elementwise stage pass."""
+    D = n * n
+    Dp = -(-D // 128) * 128
+    MT = Dp // 128
+    Rp = -(-n_rhs // 64) * 64
+    Rq = -(-n_rhs // 128) * 128
+    t4 = -(-(MT * (2 * Rp // 128)) // sms) * (2 * Dp // 64)
+    t3 = -(-(3 * MT * (Rq // 128)) // sms) * (Dp // 64) * 1.08
+    return t4, t3
+
+
+def split_product(n: int, n_rhs: int, device=None) -> str:
+    """'3m' or '4m' for this shape: the tuning cache's choice, else the
+    cost model (3M only from SPLIT_3M_MIN_DIM up and when the model gives it
+    at least 3 % less)."""
+    from . import tuning
+    if n * n < SPLIT_3M_MIN_DIM:
+        return '4m'
+    dev = engine._dev(device)
+    got = tuning.choose('redfield_split', split_class(n, n_rhs), 'split', {}, arch=tuning.arch_tag(dev))
+    if got.get('product') in ('3m', '4m'):
+        return got['product']
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    t4, t3 = split_cost(n, n_rhs, sms)
+    return '3m' if t3 < 0.97 * t4 else '4m'
+
+
+def split_class(n: int, n_rhs: int) -> str:
+    """The autotuner's class of a Redfield split shape (padded dimensions)."""
+    return 'D%d|R%d' % (-(-(n * n) // 128) * 128, -(-n_rhs // 64) * 64)
+
+
+def autotune_split(R, n_rhs: int, dt: float = 0.05, steps=(2, 6), device=None, cache=None, force=False):
+    """Time both complex-product forms on this generator and ``n_rhs``
+    right-hand sides (GPU time of ``steps[1]`` minus ``steps[0]`` RK4
+    steps, CUDA events) and cache the faster under the shape's class.
+    Returns ``(choice, times)``."""
+    from . import tuning
+    Rd, n = R
+    dev = Rd.device
+    r0 = torch.zeros((n_rhs, n, n), dtype=CDT, device=dev)
+    r0[:, 0, 0] = 1.0
+
+    def measure(cand):
+        def run(k):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(dev)
+            a.record()
+            propagate_vec_split(R, r0, dt, k, None, product=cand['product'])
+            b.record()
+            torch.cuda.synchronize(dev)
+            return a.elapsed_time(b) / 1e3
+        run(1)
+        return (run(steps[1]) - run(steps[0])) / (steps[1] - steps[0])
+
+    return tuning.tune('redfield_split', split_class(n, n_rhs), 'split', [{'product': '4m'}, {'product': '3m'}],
+                       measure, arch=tuning.arch_tag(dev), cache=cache, force=force)
 
 
 def stage_buffer_floats(n: int, n_rhs: int, n_steps: int) -> int:
@@ -196,9 +260,8 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
     """Tensor-core split-precision RK4 (``lime_redfield_rk4_split``) of
     eigenbasis density matrices (B, n, n) under the dense generator.
     ``product``: '4m' (the real block form of the complex product), '3m'
-    (three real products, ``lime_redfield_rk4_split3``) or 'auto' ('3m'
-    from Liouville dimension ``SPLIT_3M_MIN_DIM`` up); default
-    ``SPLIT_PRODUCT``.  ``stage_out``: a float32 device tensor of
+    (three real products, ``lime_redfield_rk4_split3``) or 'auto'
+    (``split_product``); default ``SPLIT_PRODUCT``.  ``stage_out``: a float32 device tensor of
     ``stage_buffer_floats(n, B, n_steps)`` elements that receives every
     stage input (for the adjoint without recomputation; block form only).
 
@@ -223,7 +286,7 @@ def propagate_vec_split(R, rho0_eb: torch.Tensor, dt: float, n_steps: int, e_eb=
     sb = _pow2_floor(8192.0 / (1.25 * pmax)) if pmax > 0 else 0
     product = SPLIT_PRODUCT if product is None else product
     if product == 'auto':
-        product = '3m' if n * n >= SPLIT_3M_MIN_DIM else '4m'
+        product = split_product(n, B, dev)
     if product not in ('3m', '4m'):
         raise ValueError("product must be '3m', '4m' or 'auto'")
     if stage_out is not None:

@@ -96,3 +96,17 @@ def test_engine_uneven_class_groups_like_the_launch():
     assert got == tuning.uneven_class([64, 64, 64, 256], [2, 2, 3, 2], 3)
     assert engine.uneven_class(H, C, 'split', pack=False) == tuning.uneven_class([64, 64, 64, 256],
                                                                                  [10, 5, 3, 2], 3)
+
+
+def test_redfield_product_cost_model():
+    """The wave-quantised cost model behind the Redfield split path's choice
+    of complex product: the 3M form at the 9216-dim, 512-RHS workload (6
+    waves of 144 chunks vs 4 of 288), the block form where the 3M tiles
+    would spill into a second wave (dim 4096, 256 RHS: measured 0.87 vs
+    0.73 ms per step)."""
+    from lime_gb300.redfield import split_class, split_cost
+    t4, t3 = split_cost(96, 512, 152)
+    assert t4 == 4 * 288 and t3 < 0.97 * t4
+    t4, t3 = split_cost(64, 256, 152)
+    assert t4 == 128 and t3 > 0.97 * t4
+    assert split_class(96, 512) == 'D9216|R512' and split_class(12, 130) == 'D256|R192'
