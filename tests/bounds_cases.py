@@ -4,8 +4,10 @@ library and once, in a child process with LIME_GB300_LIBRARY pointing at
 liblime_gb300_check.so, with the bounds-checked one.  Shapes are chosen to
 exercise padding and tile edges: ragged n (1, 5, 20, 33, 63, 70, 130), dense
 and diagonal collapse operators, dense and population observables, stored
-states, packed uneven batches, the Redfield tensor-core path with its
-split-K observable pass, the driven batched kernel and both adjoints."""
+states, packed uneven batches (grouped persistent launches and per-size
+streams), the Redfield tensor-core path in both complex-product forms with
+their split-K observable passes, the driven batched kernel and both
+adjoints."""
 import sys
 
 import numpy as np
@@ -59,8 +61,11 @@ def run_all() -> dict:
         Cs.append(c)
         R0.append(chains.ground_dm(n))
         Es.append(chains.population_ops(n)[:2])
-    o, _, r = engine.propagate_ragged(Hs, R0, 0.05, 6, Cs, Es, precision='split')
-    out['ragged'] = (torch.stack([x[:, :2] for x in o]), None, torch.cat([x.reshape(-1) for x in r]))
+    for nm, sched in (('ragged', {'mode': 'groups', 'order': 1, 'n_ctas': 0, 'pack': True}),
+                      ('ragged_streams', {'mode': 'streams', 'pack': True}),
+                      ('ragged_groups2', {'mode': 'groups', 'order': 0, 'n_ctas': 2, 'pack': False})):
+        o, _, r = engine.propagate_ragged(Hs, R0, 0.05, 6, Cs, Es, precision='split', schedule=sched)
+        out[nm] = (torch.stack([x[:, :2] for x in o]), None, torch.cat([x.reshape(-1) for x in r]))
     # Redfield: FP64 and the tensor-core path (split-K observable pass)
     rw = chains.redfield_chain(n=6, n_rhs=3, cfg=5)
     R, evecs = redfield_tensor(rw['H'], rw['a_ops'], rw['spectra'])
@@ -68,7 +73,8 @@ def run_all() -> dict:
     r0 = V.mH @ torch.as_tensor(rw['rho0'], dtype=torch.complex128, device='cuda') @ V
     E = [V.mH @ torch.as_tensor(e, device='cuda') @ V for e in chains.population_ops(6)]
     out['redfield_f64'] = propagate_vec((R.R, 6), r0, 0.05, 10, E)
-    out['redfield_split'] = propagate_vec_split((R.R, 6), r0, 0.05, 10, E)
+    out['redfield_split'] = propagate_vec_split((R.R, 6), r0, 0.05, 10, E, product='4m')
+    out['redfield_split3'] = propagate_vec_split((R.R, 6), r0, 0.05, 10, E, product='3m')
     # adjoints (FP64 and tensor-core) of the chain model
     n = 12
     eps = torch.tensor(rng.normal(0, 0.05, (2, n)), device='cuda')
