@@ -109,10 +109,27 @@ class TuneCache:
             raise
 
 
+_LOADED = {}   # cache path -> (modification time, TuneCache): one file read per change
+
+
+def _default_cache() -> TuneCache:
+    path = cache_path()
+    try:
+        mtime = os.path.getmtime(path)
+    except OSError:
+        mtime = None
+    hit = _LOADED.get(path)
+    if hit is None or hit[0] != mtime:
+        hit = (mtime, TuneCache(path))
+        _LOADED[path] = hit
+    return hit[1]
+
+
 def choose(kind: str, n_class: str, precision: str, default: dict, arch: str | None = None,
            cache: TuneCache | None = None) -> dict:
-    """The cached choice for the key, or ``default`` (no measurement)."""
-    c = cache if cache is not None else TuneCache()
+    """The cached choice for the key, or ``default`` (no measurement).  The
+    default cache file is read again only when it changes."""
+    c = cache if cache is not None else _default_cache()
     got = c.get(key(kind, n_class, precision, arch or arch_tag()))
     return got if got is not None else dict(default)
 

@@ -110,3 +110,19 @@ def test_redfield_product_cost_model():
     t4, t3 = split_cost(64, 256, 152)
     assert t4 == 128 and t3 > 0.97 * t4
     assert split_class(96, 512) == 'D9216|R512' and split_class(12, 130) == 'D256|R192'
+
+
+def test_default_cache_is_reread_only_when_it_changes(tmp_path, monkeypatch):
+    import os
+    p = tmp_path / 'tune.json'
+    monkeypatch.setenv(tuning.CACHE_ENV, str(p))
+    assert tuning.choose('k', 'c', 'split', {'d': 0}, arch='a') == {'d': 0}
+    c = tuning.TuneCache(str(p))
+    c.put(tuning.key('k', 'c', 'split', 'a'), {'d': 1})
+    c.save()
+    os.utime(p, (1, 1))                       # a distinct modification time
+    assert tuning.choose('k', 'c', 'split', {'d': 0}, arch='a') == {'d': 1}
+    c.put(tuning.key('k', 'c', 'split', 'a'), {'d': 2})
+    c.save()
+    os.utime(p, (2, 2))
+    assert tuning.choose('k', 'c', 'split', {'d': 0}, arch='a') == {'d': 2}
