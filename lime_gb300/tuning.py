@@ -9,11 +9,14 @@ at run time is chosen here by measurement and remembered in a JSON cache:
   sequence per size on concurrent streams, the tile order of the grouped
   launch (largest tiles first or as given), the persistent CTA count, and
   whether chains of dimension <= 32 are packed block-diagonally.
+* ``redfield_split`` (the tensor-core Redfield RK4): the complex product in
+  its block form or its 3M form (``redfield.autotune_split``).
 
 The cache is keyed by (kind, N-class, precision, arch): the N-class of an
 uneven batch is its multiset of padded group dimensions with bucketed
-instance counts and the collapse-operator count (``uneven_class``), the
-arch the device's compute capability.  It lives at ``$LIME_GB300_TUNE_CACHE``
+instance counts and the collapse-operator count (``uneven_class``), of a
+Redfield shape its padded Liouville dimension and right-hand-side count;
+the arch is the device's compute capability.  It lives at ``$LIME_GB300_TUNE_CACHE``
 or ``~/.cache/lime_gb300/tune.json``; a missing or unreadable file is an
 empty cache, writes are atomic (temporary file + rename).
 """
