@@ -62,7 +62,21 @@ struct Args {
   // set and of one B1 / B2 piece buffer, floats of one [B][W][np] state array
   size_t a1_bytes = kNoExtent, a2_bytes = kNoExtent, b1_bytes = kNoExtent, b2_bytes = kNoExtent;
   size_t st_floats = kNoExtent;
+  // GEMM 2 over the upper tiles of the Hermitian Z only (np a multiple of
+  // 128 with two or more row tiles): a strictly upper tile also stores its
+  // raw Z into Zg ([B][W][np], the layout of Xg), and zlower_kernel updates
+  // the elements of the lower tiles from Z[y][x] = conj(Z[x][y])
+  int zhalf = 0;
+  float* Zg = nullptr;
 };
+
+// GEMM 2 tiles per instance: all MT2 x NT, or with zhalf the upper ones,
+// (row tile mt, column block xb) with mt <= xb for each of the two
+// components
+__host__ __device__ __forceinline__ int gemm2_tiles(const Args& a) {
+  const int xbs = a.np / 128;
+  return a.zhalf ? xbs * (xbs + 1) : a.MT2 * a.NT;
+}
 
 __device__ __forceinline__ size_t inst_floats(const Args& a) { return (size_t)a.W * a.np; }
 
@@ -214,6 +228,12 @@ __device__ __forceinline__ void fused_epilogue(const Args& a, int b, int mt, int
       if (y < np) {
         float f[8];
         park8(jl, dl, f);
+        if (a.zhalf && mt < (nt * kBN % np) / 128) {
+          // raw Z of a strictly upper tile, for the transposed lower one
+          const size_t zo = (size_t)b * inst_floats(a) + (size_t)jj * np + y;
+          if (in_bounds(zo * sizeof(float), 8 * sizeof(float), a.st_floats * sizeof(float), a.status))
+            sg::st8(a.Zg + zo, f);
+        }
         assemble_f(a, b, jj, y, f);
         update8(a, b, jj, y, f, bad, range);
       }
@@ -229,10 +249,24 @@ template <bool kZ>
 __device__ __forceinline__ void gemm_tile_of(const Args& a, int local, sg::Tile& T, int& b, int& mt, int& nt) {
   const int MT = kZ ? a.MT2 : a.MT1;
   const int KC = kZ ? a.KC2 : a.KC1;
-  b = local / (MT * a.NT);
-  const int tile = local % (MT * a.NT);
-  mt = tile / a.NT;
-  nt = tile % a.NT;
+  const int per = kZ ? gemm2_tiles(a) : MT * a.NT;
+  b = local / per;
+  const int tile = local % per;
+  if (kZ && a.zhalf) {
+    // upper tiles of component comp: column block xb holds row tiles 0..xb
+    const int xbs = a.np / 128, half = xbs * (xbs + 1) / 2;
+    const int comp = tile / half;
+    int u = tile - comp * half, xb = 0;
+    while (u > xb) {
+      u -= xb + 1;
+      ++xb;
+    }
+    mt = u;
+    nt = comp * xbs + xb;
+  } else {
+    mt = tile / a.NT;
+    nt = tile % a.NT;
+  }
   const int g = a.G == 1 ? 0 : b % a.P;
   const size_t aoff = ((size_t)g * MT + mt) * KC * kPiece;
   const size_t boff = ((size_t)b * a.NT + nt) * KC * kPiece;
@@ -380,6 +414,48 @@ __global__ void __launch_bounds__(256) finish_kernel(Args a) {
   float f[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   assemble_f_tr(a, it.b, it.jj, it.y, it.tr, f);
   update8(a, it.b, it.jj, it.y, f, bad, range);
+  if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
+  if (range) atomicOr(a.status, LIME_FLAG_RANGE);
+}
+
+// The stage update of the lower tiles of Z (row tile above the column
+// block) when GEMM 2 ran over the upper ones only: Z[y][x] = conj(Z[x][y])
+// from the strictly upper tiles' raw Z in Zg, then f and the RK4 update as
+// in GEMM 2's epilogue.  One thread per run of 8 rows of one state column.
+__global__ void __launch_bounds__(256) zlower_kernel(Args a, int batch) {
+  const int np = a.np, xbs = np / 128;
+  const int pairs = xbs * (xbs - 1) / 2;               // (mt, xb) with mt > xb
+  const size_t per_inst = (size_t)2 * pairs * 128 * 16;  // components x pairs x columns x 8-row runs
+  const size_t total = (size_t)batch * per_inst;
+  bool bad = false, range = false;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    const int b = (int)(q / per_inst);
+    size_t r = q % per_inst;
+    const int run = (int)(r % 16);
+    r /= 16;
+    const int xl = (int)(r % 128);
+    r /= 128;
+    int u = (int)(r % pairs);
+    const int comp = (int)(r / pairs);
+    int mt = 1;   // lower pair u: row tile mt, column block xb < mt
+    while (u >= mt) {
+      u -= mt;
+      ++mt;
+    }
+    const int xb = u;
+    const int x = xb * 128 + xl, y = mt * 128 + run * 8;
+    const int jj = comp * np + x;
+    const float* Z = a.Zg + (size_t)b * inst_floats(a);
+    float f[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      // Re Z[y][x] = Re Z[x][y];  Im Z[y][x] = -Im Z[x][y]  (Zg[c np + x'][y'] = Z_c[y'][x'])
+      const float v = Z[(size_t)(comp * np + y + i) * np + x];
+      f[i] = comp ? -v : v;
+    }
+    assemble_f(a, b, jj, y, f);
+    update8(a, b, jj, y, f, bad, range);
+  }
   if (bad) atomicOr(a.status, LIME_FLAG_NONFINITE);
   if (range) atomicOr(a.status, LIME_FLAG_RANGE);
 }
@@ -777,6 +853,7 @@ namespace {
 
 struct LsmLayout {
   int np, W, NT, KC1, KC2, MT1, MT2, G;
+  int zhalf;                           // GEMM 2 over the upper tiles of Z only
   size_t a1, a2, r1, r2, b1, b2, st;   // bytes of one piece set / array
   size_t total;
 };
@@ -798,9 +875,10 @@ LsmLayout lsm_layout(int n, int batch, int G, int K) {
   l.b1 = (size_t)batch * l.NT * l.KC1 * sg::kPiece;
   l.b2 = (size_t)batch * l.NT * l.KC2 * sg::kPiece;
   l.st = (size_t)batch * l.W * l.np * sizeof(float);
+  l.zhalf = (K > 0 && l.np % 128 == 0 && l.np >= 256) ? 1 : 0;
   // A1 x3, A2 x3, row scales, B1 x2 pieces x2 buffers, B2 x2 pieces,
-  // X, stage input x2, Phi, Plo, Acc
-  l.total = 3 * l.a1 + 3 * l.a2 + l.r1 + l.r2 + 4 * l.b1 + 2 * l.b2 + 6 * l.st + 4096;
+  // X, stage input x2, Phi, Plo, Acc (+ Z of the upper tiles)
+  l.total = 3 * l.a1 + 3 * l.a2 + l.r1 + l.r2 + 4 * l.b1 + 2 * l.b2 + (6 + l.zhalf) * l.st + 4096;
   return l;
 }
 
@@ -875,6 +953,8 @@ int lsm_prepare(const LimeLindbladStreamDesc* d, LsmRun& r, cudaStream_t st, int
   a.Phi = reinterpret_cast<float*>(w); w += L.st;
   a.Plo = reinterpret_cast<float*>(w); w += L.st;
   a.Acc = reinterpret_cast<float*>(w); w += L.st;
+  a.zhalf = L.zhalf;
+  if (L.zhalf) { a.Zg = reinterpret_cast<float*>(w); w += L.st; }
   a.sb = ldexpf(1.f, d->scale_b_log2);
   a.inv_sb = ldexpf(1.f, -d->scale_b_log2);
   a.sy = ldexpf(1.f, d->scale_y_log2);
@@ -908,6 +988,13 @@ int lsm_prepare(const LimeLindbladStreamDesc* d, LsmRun& r, cudaStream_t st, int
   LIME_CUDA_TRY(cudaGetLastError());
   ++launches;
   return LIME_OK;
+}
+
+int lsm_zlower_grid(const lsm::Args& a, int B) {
+  const int xbs = a.np / 128;
+  const size_t runs = (size_t)B * 2 * (xbs * (xbs - 1) / 2) * 128 * 16;
+  const size_t g = (runs + 255) / 256;
+  return (int)(g < 65535 ? (g > 0 ? g : 1) : 65535);
 }
 
 // stage s with stage-input buffers cur (read) and cur ^ 1 (written)
@@ -978,7 +1065,12 @@ extern "C" int lime_lindblad_rk4_stream(const LimeLindbladStreamDesc* d, void* s
       LIME_CUDA_TRY(cudaGetLastError());
       ++launches;
       if (K > 0) {
-        lsm::gemm_kernel<true><<<B * L.MT2 * L.NT, sg::kThreads, smem, st>>>(a);
+        lsm::gemm_kernel<true><<<B * lsm::gemm2_tiles(a), sg::kThreads, smem, st>>>(a);
+        if (a.zhalf) {
+          LIME_CUDA_TRY(cudaGetLastError());
+          lsm::zlower_kernel<<<lsm_zlower_grid(a, B), 256, 0, st>>>(a, B);
+          ++launches;
+        }
       } else {
         lsm::finish_kernel<<<tb, 256, 0, st>>>(a);
       }
@@ -1048,7 +1140,7 @@ extern "C" int lime_lindblad_rk4_stream_groups(const LimeLindbladStreamDesc* des
     for (int i = 0; i < cnt; ++i) {
       const LsmRun& r = runs[o[i]];
       m.g[i] = r.a;
-      m.start[i + 1] = m.start[i] + r.B * (z ? r.L.MT2 : r.L.MT1) * r.L.NT;
+      m.start[i + 1] = m.start[i] + r.B * (z ? lsm::gemm2_tiles(r.a) : r.L.MT1 * r.L.NT);
     }
     m.n_items = m.start[cnt];
   };
@@ -1070,6 +1162,12 @@ extern "C" int lime_lindblad_rk4_stream_groups(const LimeLindbladStreamDesc* des
         lsm::gemm_groups_kernel<true><<<grid_of(m2.n_items), sg::kThreads, smem, st>>>(m2);
         LIME_CUDA_TRY(cudaGetLastError());
         ++launches;
+        for (int i = 0; i < n_groups; ++i) {
+          if (runs[i].K == 0 || !runs[i].a.zhalf) continue;
+          lsm::zlower_kernel<<<lsm_zlower_grid(runs[i].a, runs[i].B), 256, 0, st>>>(runs[i].a, runs[i].B);
+          LIME_CUDA_TRY(cudaGetLastError());
+          ++launches;
+        }
       }
       for (int i = 0; i < n_groups; ++i) {
         if (runs[i].K > 0) continue;

@@ -123,3 +123,22 @@ def test_autotune_writes_the_cache(tmp_path):
             del os.environ[tuning.CACHE_ENV]
         else:
             os.environ[tuning.CACHE_ENV] = old
+
+
+@pytest.mark.parametrize('n', [200, 256, 300, 384])
+def test_hermitian_half_gemm2_vs_fp64(n):
+    """Dense collapse operators at dimensions whose padded size is a multiple
+    of 128 with two or three row tiles (200, 256 -> 256; 384 -> 384): GEMM 2
+    runs over the upper tiles of the Hermitian Z and the lower ones are
+    updated from their transposes; 300 (padded 320) takes the full tile set.
+    Against the FP64 path, through both the single-group and the grouped
+    launch."""
+    from lime_gb300 import engine
+    H, C, R, E = _batch([n], 10 + n)
+    o64, _, r64 = engine.propagate_ragged(H, R, 0.05, 10, C, E, precision='fp64')
+    for sched in ({'mode': 'streams', 'pack': True}, {'mode': 'groups', 'order': 1, 'n_ctas': 0, 'pack': True}):
+        o, _, r = engine.propagate_ragged(H, R, 0.05, 10, C, E, precision='split', schedule=sched)
+        assert (o[0] - o64[0]).abs().max().item() < 1e-6
+        assert (r[0] - r64[0]).abs().max().item() < 1e-6
+        # the final state stays Hermitian to the split precision
+        assert (r[0] - r[0].mH).abs().max().item() < 1e-6
