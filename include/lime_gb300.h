@@ -69,11 +69,15 @@ typedef enum {
 
 /* Build Heff = H - (i/2) sum_k L_k^dag L_k  and  M = sum_k l_k l_k^dag.
  * Replaces the per-RHS products dag(l).dot(l) of lime/oqs.py:716-723.
- *   h        [B|1][n][n] complex128, stride h_stride (0 = shared)
- *   l_dense  [B|1][k_dense][n][n] complex128 dense collapse ops, or NULL
- *   l_diag   [B|1][k_diag][n]     complex128 diagonals of diagonal ops, or NULL
- *   heff     [B][n][n] complex128 out
- *   m        [B][n][n] complex128 out (zero when k_diag == 0)
+ *   h         [B|1][n][n] complex128, stride h_stride (0 = shared)
+ *   l_dense   [B|1][k_dense][n][n] complex128 dense collapse ops, or NULL
+ *   l_diag    [B|1][k_diag][n]     complex128 diagonals of diagonal ops, or NULL
+ *   heff      [B][n][n] complex128 out
+ *   m         [B][n][n] complex128 out (zero without diagonal operators)
+ *   dephasing [B|1][n] float64 site-dephasing rates r_k, or NULL: the n
+ *             operators sqrt(r_k)|k><k| given by their rates, which add
+ *             r_k to the k-th diagonal entry of sum_k L_k^dag L_k and of M;
+ *             stride dephasing_stride (0 = shared)
  */
 typedef struct {
   int32_t n, batch, k_dense, k_diag;
@@ -82,6 +86,7 @@ typedef struct {
   const double* l_diag;   int64_t l_diag_stride;
   double* heff;
   double* m;
+  const double* dephasing; int64_t dephasing_stride;
 } LimePrepareDesc;
 
 int lime_lindblad_prepare_f64(const LimePrepareDesc* d, void* stream);

@@ -62,7 +62,8 @@ class PrepareDesc(ctypes.Structure):
                 ('h', c_void_p), ('h_stride', c_int64),
                 ('l_dense', c_void_p), ('l_dense_stride', c_int64),
                 ('l_diag', c_void_p), ('l_diag_stride', c_int64),
-                ('heff', c_void_p), ('m', c_void_p)]
+                ('heff', c_void_p), ('m', c_void_p),
+                ('dephasing', c_void_p), ('dephasing_stride', c_int64)]
 
 
 class LindbladDesc(ctypes.Structure):

@@ -447,9 +447,10 @@ __global__ void __launch_bounds__(kThreads) lindblad_adjoint_f64_kernel(AdjArgs 
 // batched GEMM run before this kernel) or is absent (k_dense = 0).  For the
 // diagonal operators the diagonal sums dg[i] = sum_k |l_k[i]|^2 (which are
 // both the diagonal of sum_k L_k^dag L_k and of M) are formed once per
-// generator in shared memory, k in order; when every diagonal operator has
-// at most one nonzero entry (site dephasing) the off-diagonal terms
-// l_k[i] conj(l_k[j]) of M are exact zeros and are not summed.
+// generator in shared memory, k in order, then the site-dephasing rate r_i;
+// when every diagonal operator has at most one nonzero entry (site
+// dephasing) the off-diagonal terms l_k[i] conj(l_k[j]) of M are exact zeros
+// and are not summed.
 __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
   extern __shared__ double dg[];    // [n]
   const int b = blockIdx.x;
@@ -458,6 +459,7 @@ __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const double2* H = reinterpret_cast<const double2*>(d.h) + b * d.h_stride;
   const double2* lg = d.l_diag ? reinterpret_cast<const double2*>(d.l_diag) + b * d.l_diag_stride : nullptr;
+  const double* rate = d.dephasing ? d.dephasing + b * d.dephasing_stride : nullptr;
   double2* heff = reinterpret_cast<double2*>(d.heff) + (int64_t)b * nn;
   double2* M = reinterpret_cast<double2*>(d.m) + (int64_t)b * nn;
   __shared__ int spread;   // some l_k has two or more nonzero entries
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kThreads) prepare_kernel(LimePrepareDesc d) {
       const double2 v = lg[(int64_t)k * n + i];
       s += v.x * v.x + v.y * v.y;
     }
-    dg[i] = s;
+    dg[i] = rate ? s + rate[i] : s;
   }
   __syncthreads();
   // one warp per operator counts its nonzero entries
@@ -511,7 +513,8 @@ extern "C" int lime_lindblad_prepare_f64(const LimePrepareDesc* d, void* stream)
   if (!d || d->n <= 0 || d->batch <= 0 || d->k_dense < 0 || d->k_diag < 0) return LIME_ERR_ARG;
   if (!d->h || !d->heff || !d->m) return LIME_ERR_ARG;
   if ((d->k_dense > 0 && !d->l_dense) || (d->k_diag > 0 && !d->l_diag)) return LIME_ERR_ARG;
-  if (d->h_stride < 0 || d->l_dense_stride < 0 || d->l_diag_stride < 0) return LIME_ERR_ARG;
+  if (d->h_stride < 0 || d->l_dense_stride < 0 || d->l_diag_stride < 0 || d->dephasing_stride < 0)
+    return LIME_ERR_ARG;
   if ((size_t)d->n * sizeof(double) > 48 * 1024) return LIME_ERR_UNSUPPORTED;
   cudaStream_t st = (cudaStream_t)stream;
   if (d->k_dense > 0) {

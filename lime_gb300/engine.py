@@ -72,13 +72,17 @@ class SiteDephasing:
     def __init__(self, rates):
         self.rates = rates
 
-    def diagonal_ops(self, device) -> DiagonalOps:
+    def rates_on(self, device) -> torch.Tensor:
+        """The rates as a float64 tensor on ``device``: (n,) or (P, n)."""
         g = self.rates
         g = g.to(device=device, dtype=torch.float64) if isinstance(g, torch.Tensor) else \
             torch.as_tensor(np.asarray(g, dtype=np.float64), device=device)
         if g.dim() not in (1, 2):
             raise ValueError('SiteDephasing rates must be (n,) or (P, n)')
-        return DiagonalOps(torch.diag_embed(torch.sqrt(g)).to(CDT))
+        return g
+
+    def diagonal_ops(self, device) -> DiagonalOps:
+        return DiagonalOps(torch.diag_embed(torch.sqrt(self.rates_on(device))).to(CDT))
 
 
 class Populations:
@@ -146,10 +150,20 @@ class LindbladGenerator:
         if Hd.dim() != 3 or Hd.shape[-1] != Hd.shape[-2]:
             raise ValueError('H must be (n, n) or (P, n, n); got %s' % (tuple(Hd.shape),))
         n = Hd.shape[-1]
-        c_ops = [c.diagonal_ops(device) if isinstance(c, SiteDephasing) else c for c in (c_ops or [])]
+        c_ops = list(c_ops or [])
+        # site dephasing enters the preparation kernel as its rates
+        rates = [c.rates_on(device) for c in c_ops if isinstance(c, SiteDephasing)]
+        c_ops = [c for c in c_ops if not isinstance(c, SiteDephasing)]
         packed = [as_device(c.l, device) for c in c_ops if isinstance(c, DiagonalOps)]
         ops = [as_device(c, device) for c in c_ops if not isinstance(c, DiagonalOps)]
         P = Hd.shape[0]
+        for r in rates:
+            if r.shape[-1] != n:
+                raise ValueError('SiteDephasing rates must be (%d,) or (P, %d)' % (n, n))
+            if r.dim() == 2:
+                if P not in (1, r.shape[0]):
+                    raise ValueError('inconsistent batch sizes in H and c_ops')
+                P = r.shape[0]
         for p in packed:
             if p.shape[-1] != n or p.dim() not in (2, 3):
                 raise ValueError('DiagonalOps.l must be (K, %d) or (P, K, %d)' % (n, n))
@@ -184,7 +198,13 @@ class LindbladGenerator:
             parts = ([] if lg is None else [lg]) + [p if p.dim() == 3 else p.unsqueeze(0) for p in packed]
             if any(x.shape[0] != 1 for x in parts):
                 parts = [x.expand((P,) + x.shape[1:]) for x in parts]
-            lg = torch.cat(parts, 1).contiguous()
+            lg = parts[0].contiguous() if len(parts) == 1 else torch.cat(parts, 1).contiguous()
+        rate = None
+        if rates:
+            rate = rates[0]
+            for r in rates[1:]:
+                rate = rate + r
+            rate = (rate if rate.dim() == 2 else rate.unsqueeze(0)).contiguous()
         Hs = Hd.contiguous()
         heff = torch.empty((P, n, n), dtype=CDT, device=device)
         m = torch.empty((P, n, n), dtype=CDT, device=device)
@@ -197,12 +217,15 @@ class LindbladGenerator:
             d.l_dense, d.l_dense_stride = ld.data_ptr(), (0 if ld.shape[0] == 1 else d.k_dense * n * n)
         if lg is not None:
             d.l_diag, d.l_diag_stride = lg.data_ptr(), (0 if lg.shape[0] == 1 else d.k_diag * n)
+        if rate is not None:
+            d.dephasing, d.dephasing_stride = rate.data_ptr(), (0 if rate.shape[0] == 1 else n)
         d.heff, d.m = heff.data_ptr(), m.data_ptr()
         nat.check(lib.lime_lindblad_prepare_f64(d, _stream_ptr()), 'lime_lindblad_prepare_f64')
-        if ld is not None and ld.shape[0] == 1 and P > 1:
-            pass  # stride 0 handles sharing
-        return LindbladGenerator(n=n, P=P, heff=heff, m=(m if lg is not None else None),
-                                 l_dense=ld, k_dense=d.k_dense, shared=shared)
+        gen = LindbladGenerator(n=n, P=P, heff=heff, m=(m if lg is not None or rate is not None else None),
+                                l_dense=ld, k_dense=d.k_dense, shared=shared)
+        if lg is None and rate is not None:
+            gen.split_cache['m_diagonal'] = True   # site dephasing alone: M = diag(rates)
+        return gen
 
 
 def hermitian_parts(rho: torch.Tensor):
@@ -297,7 +320,7 @@ def split_supported(gen: LindbladGenerator) -> str | None:
             why = 'dimension %d > %d' % (gen.n, SPLIT_MAX_N)
         elif gen.k_dense:
             why = 'dense (non-diagonal) collapse operators'
-        elif gen.m is not None and not is_diagonal(gen.m):
+        elif gen.m is not None and not c.get('m_diagonal') and not is_diagonal(gen.m):
             why = 'diagonal collapse operators with a non-diagonal M = sum_k l_k l_k^dag'
         c['why'] = why
     return c['why']
@@ -368,6 +391,8 @@ def _split_obs(e_ops, n, P, device):
     """(mode, n_obs, tensor, stride) for the split kernel.  Site
     populations given as host arrays are recognised on the host (no device
     round trip); device tensors are compared on the device."""
+    if isinstance(e_ops, SplitObs):
+        return e_ops.spec
     if isinstance(e_ops, Populations):
         if e_ops.count > n:
             raise ValueError('%d populations of a %d-dimensional system' % (e_ops.count, n))
@@ -527,7 +552,7 @@ def _run_stream(gen: LindbladGenerator, rho: torch.Tensor, dt: float, n_steps: i
     l_shared = gen.l_dense is None or gen.l_dense.shape[0] == 1
     # a diagonal M (pure dephasing) goes in as its real diagonal
     m_diag = None
-    if gen.m is not None and is_diagonal(gen.m):
+    if gen.m is not None and (gen.split_cache.get('m_diagonal') or is_diagonal(gen.m)):
         m_diag = torch.diagonal(gen.m, dim1=-2, dim2=-1).real.contiguous()
     G = 1 if (heff_shared and l_shared) else param_batch
     wsb = lib.lime_lindblad_stream_workspace(n, B, G, K)
@@ -701,6 +726,204 @@ def propagate(gen: LindbladGenerator, rho0, dt: float, n_steps: int, e_ops=None,
     """
     return _launch(gen, rho0, dt, n_steps, e_ops, states_every, precision, trace_tol,
                    obs_every, events, drive)(check)
+
+
+# A host batch for the batched split kernel runs as a pipeline of launches
+# over instance ranges: the generators of the ranges are prepared while the
+# later ranges upload, and the copy back of range c overlaps the kernel on
+# range c + 1.  The kernel keeps SPLIT_CTAS_PER_SM CTAs per SM resident (its
+# launch default) and each CTA propagates one instance at a time, so a
+# "round" is 2 x SMs instances; the ranges are whole rounds (the partial
+# round last), which keeps the number of rounds, and so the kernel time,
+# that of a single launch.
+SPLIT_CTAS_PER_SM = 2
+PIPELINE_MIN_ROUNDS = 3      # host batches of fewer rounds run as one launch
+PIPELINE_ROUNDS = 4          # rounds per range
+
+
+class SplitObs:
+    """Observables already resolved for the batched split kernel (the
+    ``(mode, n_obs, tensor, stride)`` of ``_split_obs``), shared by the
+    launches of a pipeline so that none of them inspects the operators."""
+
+    def __init__(self, spec):
+        self.spec = spec
+
+
+def pipeline_chunks(P: int, slots: int, rounds: int = PIPELINE_ROUNDS) -> list:
+    """Instance ranges [(lo, hi), ...] of a pipelined batch of P instances:
+    ``rounds`` whole rounds of ``slots`` instances per range, the last whole
+    rounds, then the partial last round alone (its copy back is the
+    pipeline's tail)."""
+    if P < 0 or slots < 1 or rounds < 1:
+        raise ValueError('pipeline_chunks needs P >= 0 and positive slots / rounds')
+    full, rem = divmod(P, slots)
+    out = [(lo, min(lo + rounds * slots, full * slots)) for lo in range(0, full * slots, rounds * slots)]
+    if rem:
+        out.append((full * slots, P))
+    return out
+
+
+def _ndim(a) -> int:
+    if isinstance(a, torch.Tensor):
+        return a.dim()
+    if hasattr(a, 'toarray'):
+        return 2
+    return int(np.ndim(a))
+
+
+def _per_instance(a, P: int):
+    """True if operand ``a`` (an array, SiteDephasing or DiagonalOps) has a
+    leading instance axis of length P, False if it is shared, None if it is
+    neither (left to the one-launch path to report)."""
+    if isinstance(a, SiteDephasing):
+        x, nd = a.rates, 2
+    elif isinstance(a, DiagonalOps):
+        x, nd = a.l, 3
+    else:
+        x, nd = a, 3
+    d = _ndim(x)
+    if d == nd - 1:
+        return False
+    if d != nd:
+        return None
+    lead = int(x.shape[0]) if hasattr(x, 'shape') else len(x)
+    return True if lead == P else (False if lead == 1 else None)
+
+
+def _upload(a, device, lo=None, hi=None):
+    """Device copy (asynchronous on the current stream for pinned memory) of
+    a host operand, instances lo:hi of it when given."""
+    def dev(x, dtype):
+        if hasattr(x, 'toarray'):
+            x = x.toarray()
+        if lo is not None:
+            x = x[lo:hi]
+        t = x if isinstance(x, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(x))
+        return t.to(device=device, dtype=dtype, non_blocking=True)
+    if isinstance(a, SiteDephasing):
+        return SiteDephasing(dev(a.rates, torch.float64))
+    if isinstance(a, DiagonalOps):
+        return DiagonalOps(dev(a.l, CDT))
+    return dev(a, CDT)
+
+
+_PIPE_STREAMS = {}
+
+
+def _pipeline_streams(device):
+    """The pipeline's upload, preparation and copy-back streams of a device,
+    created once: the caching allocator keeps freed blocks per stream, so
+    fresh streams on every call would allocate every buffer anew."""
+    k = device.index if device.index is not None else torch.cuda.current_device()
+    if k not in _PIPE_STREAMS:
+        _PIPE_STREAMS[k] = tuple(torch.cuda.Stream(device) for _ in range(3))
+    return _PIPE_STREAMS[k]
+
+
+def propagate_host_pipelined(H, rho0, c_ops, e_ops, dt: float, n_steps: int, obs_every: int = 1,
+                             trace_tol: float | None = None, device=None):
+    """A batch given in host memory on the batched split kernel, as a
+    pipeline of launches over instance ranges (``pipeline_chunks``).
+
+    Four streams: uploads of each range's operands, generator preparation
+    (which reads max |Heff| of its range back to the host), the kernels (the
+    caller's current stream, in range order) and the copies of each range's
+    observables and final states into page-locked host tensors.  The ranges'
+    generators are prepared while the uploads land; the copies back overlap
+    the propagation of the later ranges.  Returns
+    ``(obs, rho)``, host tensors (P, n_steps // obs_every, n_obs) and
+    (P, n, n), or None when the batch does not qualify: the kernel does not
+    handle the generator, rho0 is not Hermitian, an observable is per
+    instance, or the batch is shorter than PIPELINE_MIN_ROUNDS rounds.  The
+    caller then runs it as one launch.
+
+    Each range's A operand takes its own power-of-two scale from its own
+    max |Heff|; where the ranges' scales agree with the single launch's the
+    results are bitwise those of the single launch, otherwise they differ
+    within the split path's rounding."""
+    if not torch.cuda.is_available() or n_steps < 1 or obs_every < 1:
+        return None
+    if not hasattr(H, 'shape') or (isinstance(H, torch.Tensor) and H.device.type != 'cpu'):
+        return None
+    if _ndim(H) != 3:
+        return None
+    P, n = int(H.shape[0]), int(H.shape[-1])
+    if n > SPLIT_MAX_N or tuple(H.shape[-2:]) != (n, n):
+        return None
+    device = _dev(device)
+    slots = SPLIT_CTAS_PER_SM * torch.cuda.get_device_properties(device).multi_processor_count
+    if -(-P // slots) < PIPELINE_MIN_ROUNDS:
+        return None
+    c_ops = list(c_ops or [])
+    per = [_per_instance(a, P) for a in c_ops]
+    rho_per = _per_instance(rho0, P)
+    if any(p is None for p in per) or rho_per is None:
+        return None
+    if not isinstance(e_ops, Populations) and e_ops and any(_ndim(e) != 2 for e in e_ops):
+        return None
+    if not _host_hermitian(rho0):
+        return None
+    nat.require_device()
+    comp = torch.cuda.current_stream(device)
+    up, prep, down = _pipeline_streams(device)
+    spec = _split_obs(e_ops if e_ops is not None else [], n, 1, device)
+    T, n_obs = n_steps // obs_every, spec[1]
+    obs_h = torch.empty((P, T, n_obs), dtype=CDT, pin_memory=True)
+    rho_h = torch.empty((P, n, n), dtype=CDT, pin_memory=True)
+    chunks = pipeline_chunks(P, slots)
+    # every upload is enqueued first, in range order: range c lands while the
+    # generators of the ranges before it are prepared
+    inputs = []
+    with torch.cuda.stream(up):
+        shared = [None if p else _upload(a, device) for a, p in zip(c_ops, per)]
+        rho_shared = None if rho_per else _upload(rho0, device)
+        for lo, hi in chunks:
+            ev = torch.cuda.Event()
+            Hc = _upload(H, device, lo, hi)
+            cc = [_upload(a, device, lo, hi) if p else s for a, p, s in zip(c_ops, per, shared)]
+            rc = _upload(rho0, device, lo, hi) if rho_per else rho_shared
+            ev.record(up)
+            inputs.append((ev, Hc, cc, rc))
+    # each range's generator as soon as its upload lands.  All of them come
+    # before the first propagation: the propagation kernel keeps every SM
+    # busy, so preparation kernels queued behind it would wait for it
+    gens = []
+    for i, (ev_in, Hc, cc, rc) in enumerate(inputs):
+        with torch.cuda.stream(prep):
+            prep.wait_event(ev_in)
+            gen = LindbladGenerator.build(Hc, cc, device=device)
+            if split_supported(gen) is not None:
+                if i:
+                    raise RuntimeError('pipelined batch: range %d needs another kernel' % i)
+                torch.cuda.synchronize(device)
+                return None
+            split_operands(gen)          # reads max |Heff| of the range back
+        gens.append(gen)
+    comp.wait_stream(prep)               # (prep waited for every upload)
+    # the propagations back to back; each range's results are copied back
+    # while the next range runs
+    keep, finishers = [], []
+    for (lo, hi), gen, (_, _, _, rc) in zip(chunks, gens, inputs):
+        ev_done = torch.cuda.Event()
+        with torch.cuda.stream(comp):
+            fin = _launch(gen, rc, dt, n_steps, SplitObs(spec), 0, 'split', trace_tol, obs_every,
+                          hermitian=True)
+            o, _, r = fin(False)
+            ev_done.record(comp)
+        with torch.cuda.stream(down):
+            down.wait_event(ev_done)
+            obs_h[lo:hi].copy_(o, non_blocking=True)
+            rho_h[lo:hi].copy_(r, non_blocking=True)
+        # every range's buffers live until the last copy back has finished:
+        # a buffer freed early could be handed to another stream mid-use
+        keep.append((o, r))
+        finishers.append(fin)
+    down.synchronize()
+    for fin in finishers:
+        fin(True)                        # raises on a kernel status flag
+    del keep, inputs, gens
+    return obs_h, rho_h
 
 
 def _dims(a):

@@ -79,6 +79,14 @@ def _lindblad(H, rho0, c_ops, e_ops=None, Nt=1, dt=0.005, return_result=True,
     batched = _is_batched(H, rho0) or any(
         (isinstance(c, engine.DiagonalOps) and np.ndim(c.l) == 3) or
         (isinstance(c, engine.SiteDephasing) and np.ndim(c.rates) == 2) for c in (c_ops or []))
+    if return_result and precision == 'split' and not store_states:
+        # a host batch: uploads, launches and copies back overlapped per instance range
+        got = engine.propagate_host_pipelined(H, rho0, c_ops, e_ops, dt, Nt, obs_every=nout)
+        if got is not None:
+            res = Result(dt=dt, Nt=Nt, rho0=rho0, t0=0.0, nout=nout)
+            res.observables = got[0].numpy()
+            res.rholist = got[1].numpy()
+            return res
     gen = engine.LindbladGenerator.build(H, c_ops)
     if return_result:
         obs, states, rho = engine.propagate(gen, rho0, dt, Nt, e_ops,

@@ -35,3 +35,50 @@ def test_zgemm_wrapper_rejects_bad_operands():
         zl.bmm(a, a)                                   # not on a CUDA device
     with pytest.raises(ValueError):
         zl.bmm(torch.zeros((2, 2), dtype=torch.complex128), a)   # not 3-d
+
+
+@pytest.mark.parametrize('P', [0, 1, 151, 304, 305, 912, 929, 4096, 4100, 12345])
+@pytest.mark.parametrize('slots', [1, 7, 304])
+def test_pipeline_ranges(P, slots):
+    """The ranges tile [0, P) in order; all but a partial last one are whole
+    rounds, at most four; the number of rounds is that of one launch."""
+    from lime_gb300.engine import pipeline_chunks
+    ch = pipeline_chunks(P, slots)
+    lo = 0
+    rounds = 0
+    for a, b in ch:
+        assert a == lo and b > a
+        size = b - a
+        if b < P or P % slots == 0:
+            assert size % slots == 0 and size // slots <= 4
+        rounds += -(-size // slots)
+        lo = b
+    assert lo == P
+    assert rounds == -(-P // slots)
+    if P % slots:
+        assert ch[-1] == (P - P % slots, P)                # the partial round alone
+
+
+def test_pipeline_operand_classification():
+    from lime_gb300.engine import DiagonalOps, SiteDephasing, _per_instance
+    P, n = 10, 4
+    assert _per_instance(np.zeros((P, n, n)), P) is True
+    assert _per_instance(np.zeros((1, n, n)), P) is False
+    assert _per_instance(np.zeros((n, n)), P) is False
+    assert _per_instance(np.zeros((3, n, n)), P) is None
+    assert _per_instance(SiteDephasing(np.ones((P, n))), P) is True
+    assert _per_instance(SiteDephasing(np.ones(n)), P) is False
+    assert _per_instance(DiagonalOps(np.ones((P, 2, n))), P) is True
+    assert _per_instance(DiagonalOps(np.ones((2, n))), P) is False
+    assert _per_instance(torch.zeros((P, n, n)), P) is True
+
+
+def test_pipeline_needs_a_gpu_batch_to_engage():
+    """Without a GPU (or for a device H) the pipeline declines and the caller
+    takes the one-launch path."""
+    from lime_gb300.engine import Populations, SiteDephasing, propagate_host_pipelined
+    if torch.cuda.is_available():
+        pytest.skip('checks the CPU-only answer')
+    H = np.zeros((4096, 8, 8), dtype=np.complex128)
+    assert propagate_host_pipelined(H, np.eye(8) / 8, [SiteDephasing(np.ones(8))], Populations(8),
+                                    0.05, 4) is None
