@@ -273,9 +273,53 @@ __host__ __device__ __forceinline__ int a_piece_index(int piece, int qq, int h, 
 // of a row (the coalesced copies) stay one contiguous 128-byte run.
 __device__ __forceinline__ int stage_index(int i, int j) { return i * kN + (j ^ (i & 7)); }
 
+// 2^ea a_elem(...) with the power-of-two scaling as an exponent-field add
+// (fpconv::scale_pow2; zeros keep their sign), bit-identical to the FP64
+// product.
+__device__ __forceinline__ double a_elem_scaled(const double2* heff, int n, int i, int k, bool xi_row, int ea) {
+  const double x = a_elem(heff, n, i, k, xi_row);
+  return (fpconv::bits64(x) << 1) == 0 ? x : fpconv::scale_pow2(x, ea);
+}
+
+// a_row_max and a_pieces_row without the FP64 pipe: the scaling by
+// 2^ea = sa through a_elem_scaled and the float pair (float) x,
+// (float)(x - (float) x) through fpconv::split_f64, both bit-identical to
+// the FP64 instructions, so the pieces are those of the kernel's own split.
+// For the stand-alone preparation kernel, whose time is otherwise the FP64
+// pipe's (a few operations per clock per SM on this part).
+__device__ __forceinline__ float a_row_max_int(const double2* heff, int n, int i, bool xi_row, int ea) {
+  float m = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < 128; ++k) {
+    float hi, lo;
+    fpconv::split_f64(a_elem_scaled(heff, n, i, k, xi_row, ea), hi, lo);
+    m = fmaxf(m, fabsf(hi));
+  }
+  return m;
+}
+
+__device__ __forceinline__ void a_pieces_row_int(const double2* heff, int n, int i, bool xi_row, int h, int qq,
+                                                 int ea, float magic, float qmax, uint32_t (&p0)[16],
+                                                 uint32_t (&p1)[16], uint32_t (&p2)[16]) {
+#pragma unroll
+  for (int c = 0; c < 16; ++c) {
+    const int k = 64 * h + 32 * qq + 2 * c;
+    __half x0, x1, x2, y0, y1, y2;
+    float uh, ul, wh, wl;
+    fpconv::split_f64(a_elem_scaled(heff, n, i, k, xi_row, ea), uh, ul);
+    fpconv::split_f64(a_elem_scaled(heff, n, i, k + 1, xi_row, ea), wh, wl);
+    split_a32(uh, ul, magic, qmax, x0, x1, x2);
+    split_a32(wh, wl, magic, qmax, y0, y1, y2);
+    p0[c] = pack_half2(x0, y0);
+    p1[c] = pack_half2(x1, y1);
+    p2[c] = pack_half2(x2, y2);
+  }
+}
+
 // One CTA per generator, the thread layout of the propagation kernel.
+// sa = 2^ea is a normal power of two (|ea| <= 60).
 __global__ void __launch_bounds__(kThreads) prepare_a_kernel(const double2* heff, int64_t heff_stride, int n,
-                                                              double sa, uint4* out) {
+                                                              int ea, uint4* out) {
   const int t = threadIdx.x, warp = t >> 5;
   const int r = (warp & 3) * 32 + (t & 31), h = warp >> 2;
   const bool xi_row = r >= 64;
@@ -283,11 +327,11 @@ __global__ void __launch_bounds__(kThreads) prepare_a_kernel(const double2* heff
   const double2* H = heff + (int64_t)blockIdx.x * heff_stride;
   uint4* o = out + (int64_t)blockIdx.x * kAPieceU4;
   float magic, qmax;
-  a_row_quantum(a_row_max(H, n, i, xi_row, sa), magic, qmax);
+  a_row_quantum(a_row_max_int(H, n, i, xi_row, ea), magic, qmax);
 #pragma unroll 1
   for (int qq = 0; qq < 2; ++qq) {
     uint32_t p[3][16];
-    a_pieces_row(H, n, i, xi_row, h, qq, sa, magic, qmax, p[0], p[1], p[2]);
+    a_pieces_row_int(H, n, i, xi_row, h, qq, ea, magic, qmax, p[0], p[1], p[2]);
 #pragma unroll
     for (int piece = 0; piece < 3; ++piece)
 #pragma unroll
@@ -908,7 +952,7 @@ extern "C" int lime_lindblad_split_prepare(const LimeLindbladSplitPrepareDesc* d
     return LIME_ERR_ARG;
   if (d->out_bytes < lime_lindblad_split_prepared_bytes(d->n, d->count)) return LIME_ERR_WORKSPACE;
   split::prepare_a_kernel<<<d->count, split::kThreads, 0, (cudaStream_t)stream>>>(
-      reinterpret_cast<const double2*>(d->heff), d->heff_stride, d->n, ldexp(1.0, d->scale_a_log2),
+      reinterpret_cast<const double2*>(d->heff), d->heff_stride, d->n, (int)d->scale_a_log2,
       reinterpret_cast<uint4*>(d->out));
   LIME_CUDA_TRY(cudaGetLastError());
   count_launch();

@@ -826,22 +826,20 @@ def propagate_host_pipelined(H, rho0, c_ops, e_ops, dt: float, n_steps: int, obs
     """A batch given in host memory on the batched split kernel, as a
     pipeline of launches over instance ranges (``pipeline_chunks``).
 
-    Four streams: uploads of each range's operands, generator preparation
-    (which reads max |Heff| of its range back to the host), the kernels (the
-    caller's current stream, in range order) and the copies of each range's
-    observables and final states into page-locked host tensors.  The ranges'
-    generators are prepared while the uploads land; the copies back overlap
-    the propagation of the later ranges.  Returns
+    Four streams: uploads of each range's operands, generator preparation,
+    the kernels (the caller's current stream, in range order) and the copies
+    of each range's observables and final states into page-locked host
+    tensors.  The ranges' generators are prepared while the uploads land;
+    the copies back overlap the propagation of the later ranges.  Returns
     ``(obs, rho)``, host tensors (P, n_steps // obs_every, n_obs) and
     (P, n, n), or None when the batch does not qualify: the kernel does not
     handle the generator, rho0 is not Hermitian, an observable is per
     instance, or the batch is shorter than PIPELINE_MIN_ROUNDS rounds.  The
     caller then runs it as one launch.
 
-    Each range's A operand takes its own power-of-two scale from its own
-    max |Heff|; where the ranges' scales agree with the single launch's the
-    results are bitwise those of the single launch, otherwise they differ
-    within the split path's rounding."""
+    Every range's A operand takes the power-of-two scale of the whole
+    batch's max |Heff| (one read back to the host), so the results are
+    bitwise those of the single launch."""
     if not torch.cuda.is_available() or n_steps < 1 or obs_every < 1:
         return None
     if not hasattr(H, 'shape') or (isinstance(H, torch.Tensor) and H.device.type != 'cpu'):
@@ -885,10 +883,8 @@ def propagate_host_pipelined(H, rho0, c_ops, e_ops, dt: float, n_steps: int, obs
             rc = _upload(rho0, device, lo, hi) if rho_per else rho_shared
             ev.record(up)
             inputs.append((ev, Hc, cc, rc))
-    # each range's generator as soon as its upload lands.  All of them come
-    # before the first propagation: the propagation kernel keeps every SM
-    # busy, so preparation kernels queued behind it would wait for it
-    gens = []
+    # each range's generator as soon as its upload lands, and its max |Heff|
+    gens, amax = [], []
     for i, (ev_in, Hc, cc, rc) in enumerate(inputs):
         with torch.cuda.stream(prep):
             prep.wait_event(ev_in)
@@ -898,8 +894,17 @@ def propagate_host_pipelined(H, rho0, c_ops, e_ops, dt: float, n_steps: int, obs
                     raise RuntimeError('pipelined batch: range %d needs another kernel' % i)
                 torch.cuda.synchronize(device)
                 return None
-            split_operands(gen)          # reads max |Heff| of the range back
+            amax.append(gen.heff.abs().amax())
         gens.append(gen)
+    # one read back for the whole batch: every range's A operand takes the
+    # scale of the batch's max |Heff|, the scale of a single launch.  The A
+    # operands are prepared before the first propagation: the propagation
+    # kernel keeps every SM busy, so kernels queued behind it would wait
+    with torch.cuda.stream(prep):
+        top = float(torch.stack(amax).max().item())
+        for gen in gens:
+            gen.split_cache['amax'] = top
+            split_operands(gen)
     comp.wait_stream(prep)               # (prep waited for every upload)
     # the propagations back to back; each range's results are copied back
     # while the next range runs
@@ -922,7 +927,7 @@ def propagate_host_pipelined(H, rho0, c_ops, e_ops, dt: float, n_steps: int, obs
     down.synchronize()
     for fin in finishers:
         fin(True)                        # raises on a kernel status flag
-    del keep, inputs, gens
+    del keep, inputs, gens, amax
     return obs_h, rho_h
 
 

@@ -147,12 +147,22 @@ def test_hermiticity_flag_and_untouched_input():
     assert (r2 - r64).abs().max().item() < POP_TOL
 
 
-def test_prepared_operand_matches_in_kernel_split():
-    """The A operand prepared once per generator and the one split inside
-    the kernel are the same pieces: bitwise identical results."""
+@pytest.mark.parametrize('entries', ['ensemble', 'wide'])
+def test_prepared_operand_matches_in_kernel_split(entries):
+    """The A operand prepared once per generator (integer conversions) and
+    the one split inside the kernel (FP64 instructions) are the same pieces:
+    bitwise identical results.  'wide': Hamiltonian entries over 30 decades,
+    exact zeros among them, so that the conversions' fallback range (scaled
+    entries below 2^-74) is exercised too."""
     from lime_gb300 import _native, engine
     lib = _native.require_device()
     w, c_ops = _ensemble(40, 5, 50)
+    if entries == 'wide':
+        rng = np.random.default_rng(5)
+        a = (rng.normal(size=(5, 40, 40)) + 1j * rng.normal(size=(5, 40, 40))) * \
+            10.0 ** rng.uniform(-30, 0, (5, 40, 40))
+        a[rng.random((5, 40, 40)) < 0.3] = 0
+        w['H'] = 0.1 * (a + np.conj(np.swapaxes(a, 1, 2)))
     gen = engine.LindbladGenerator.build(w['H'], c_ops)
     prep = engine.split_operands(gen)
     rho = torch.as_tensor(np.broadcast_to(w['rho0'], (5, 40, 40)).copy(), device='cuda')
