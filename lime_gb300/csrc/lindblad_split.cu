@@ -316,22 +316,39 @@ __device__ __forceinline__ void a_pieces_row_int(const double2* heff, int n, int
   }
 }
 
+// The generator staged in shared memory: kN rows of kPrepLd double2, zero
+// beyond n.  The padded row puts 8 consecutive rows 16 bytes apart in the
+// banks, so a warp's per-thread reads of 32 rows at one column are
+// conflict-free.
+constexpr int kPrepLd = kN + 1;
+constexpr size_t kPrepSmem = (size_t)kN * kPrepLd * sizeof(double2);   // 66,560 bytes
+
 // One CTA per generator, the thread layout of the propagation kernel.
-// sa = 2^ea is a normal power of two (|ea| <= 60).
+// sa = 2^ea is a normal power of two (|ea| <= 60).  The generator is read
+// from global memory once, coalesced, into shared memory; every thread then
+// reads its block row there (with stride kPrepLd and every index below
+// kN < kPrepLd, a_elem's bound never cuts and the zero fill stands for the
+// entries beyond n).
 __global__ void __launch_bounds__(kThreads) prepare_a_kernel(const double2* heff, int64_t heff_stride, int n,
                                                               int ea, uint4* out) {
+  extern __shared__ double2 hs[];   // [kN][kPrepLd]
   const int t = threadIdx.x, warp = t >> 5;
   const int r = (warp & 3) * 32 + (t & 31), h = warp >> 2;
   const bool xi_row = r >= 64;
   const int i = r & 63;
   const double2* H = heff + (int64_t)blockIdx.x * heff_stride;
   uint4* o = out + (int64_t)blockIdx.x * kAPieceU4;
+  for (int e = t; e < kN * kN; e += kThreads) {
+    const int ei = e / kN, ej = e % kN;
+    hs[ei * kPrepLd + ej] = (ei < n && ej < n) ? H[(int64_t)ei * n + ej] : make_double2(0.0, 0.0);
+  }
+  __syncthreads();
   float magic, qmax;
-  a_row_quantum(a_row_max_int(H, n, i, xi_row, ea), magic, qmax);
+  a_row_quantum(a_row_max_int(hs, kPrepLd, i, xi_row, ea), magic, qmax);
 #pragma unroll 1
   for (int qq = 0; qq < 2; ++qq) {
     uint32_t p[3][16];
-    a_pieces_row_int(H, n, i, xi_row, h, qq, ea, magic, qmax, p[0], p[1], p[2]);
+    a_pieces_row_int(hs, kPrepLd, i, xi_row, h, qq, ea, magic, qmax, p[0], p[1], p[2]);
 #pragma unroll
     for (int piece = 0; piece < 3; ++piece)
 #pragma unroll
@@ -951,7 +968,9 @@ extern "C" int lime_lindblad_split_prepare(const LimeLindbladSplitPrepareDesc* d
   if ((reinterpret_cast<uintptr_t>(d->heff) & 15) != 0 || (reinterpret_cast<uintptr_t>(d->out) & 15) != 0)
     return LIME_ERR_ARG;
   if (d->out_bytes < lime_lindblad_split_prepared_bytes(d->n, d->count)) return LIME_ERR_WORKSPACE;
-  split::prepare_a_kernel<<<d->count, split::kThreads, 0, (cudaStream_t)stream>>>(
+  LIME_CUDA_TRY(cudaFuncSetAttribute(split::prepare_a_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)split::kPrepSmem));
+  split::prepare_a_kernel<<<d->count, split::kThreads, split::kPrepSmem, (cudaStream_t)stream>>>(
       reinterpret_cast<const double2*>(d->heff), d->heff_stride, d->n, (int)d->scale_a_log2,
       reinterpret_cast<uint4*>(d->out));
   LIME_CUDA_TRY(cudaGetLastError());
