@@ -911,7 +911,8 @@ def e2e_leg(wl, K, path, dev):
             'h2d_bytes_per_step': h2d / K, 'd2h_bytes_per_step': d2h / K,
             'api': 'lime_gb300.oqs.Lindblad_solver.evolve (pinned host H and dephasing rates '
                    '(SiteDephasing), site populations (Populations), numpy Result out: '
-                   'observables and the final states)'}
+                   'observables and the final states; uploads, launches and copies back '
+                   'pipelined over instance ranges)'}
 
 
 REF_INNER = 8   # RK4 steps per host core in one reference-arm step
