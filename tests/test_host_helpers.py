@@ -82,3 +82,29 @@ def test_pipeline_needs_a_gpu_batch_to_engage():
     H = np.zeros((4096, 8, 8), dtype=np.complex128)
     assert propagate_host_pipelined(H, np.eye(8) / 8, [SiteDephasing(np.ones(8))], Populations(8),
                                     0.05, 4) is None
+
+
+def test_pipeline_upload_slices_each_operand_form():
+    """_upload (here onto the CPU device) takes instances lo:hi of a per-
+    instance operand in each accepted form and converts it to the kernels'
+    dtypes; a shared operand is copied whole."""
+    import scipy.sparse as sp
+    from lime_gb300.engine import DiagonalOps, SiteDephasing, _upload
+    cpu = torch.device('cpu')
+    P, n = 6, 3
+    H = np.arange(P * n * n, dtype=np.float64).reshape(P, n, n)
+    got = _upload(H, cpu, 2, 5)
+    assert got.dtype == torch.complex128 and tuple(got.shape) == (3, n, n)
+    assert np.array_equal(got.numpy().real, H[2:5])
+    got = _upload(torch.as_tensor(H).to(torch.complex128), cpu, 1, 2)
+    assert np.array_equal(got.numpy().real, H[1:2])
+    r = _upload(SiteDephasing(np.ones((P, n)) * np.arange(P)[:, None]), cpu, 3, 6)
+    assert isinstance(r, SiteDephasing) and r.rates.dtype == torch.float64
+    assert np.array_equal(r.rates.numpy()[:, 0], [3, 4, 5])
+    l = _upload(DiagonalOps(np.ones((P, 2, n))), cpu, 0, 4)
+    assert isinstance(l, DiagonalOps) and tuple(l.l.shape) == (4, 2, n) and l.l.dtype == torch.complex128
+    s = _upload(sp.csr_matrix(np.eye(n)), cpu)
+    assert np.array_equal(s.numpy(), np.eye(n))
+    # a non-contiguous per-instance array is sliced before it is made contiguous
+    Hf = np.asfortranarray(H)
+    assert np.array_equal(_upload(Hf, cpu, 4, 6).numpy().real, H[4:6])
